@@ -1,0 +1,237 @@
+/*
+ * sdg_advect.h -- C ABI of the GB300 (sm_103a) implementation of the SCALE-DG
+ * 3D DG advection hot path: upwind face flux, sum-factorised divergence, lift,
+ * and the SSP-RK3 stage update.
+ *
+ * Conventions, identical to the reference's Fortran arrays:
+ *   - every array is column-major (first index fastest) and is passed by
+ *     address, with no descriptor;
+ *   - a field is (Np, NeA) with node n = i + (j-1)*Nq + (k-1)*Nq^2; the
+ *     first Np*Ne values are the owned elements, and the halo slots follow;
+ *   - VMapM / VMapP / halo_src_map hold 1-BASED flat DOF indices;
+ *   - scalars are passed by value (Fortran: bind(C) with the value
+ *     attribute);
+ *   - `stream` arguments are cudaStream_t passed as void* (NULL means the
+ *     legacy default stream).
+ *
+ * Every entry point returns an int status: SDG_OK (0) on success, a negative
+ * SDG_ERR_* code otherwise.  It never aborts the process.  sdg_last_error()
+ * returns a message for the calling thread's last failure.  Entry points
+ * that take host pointers copy through device memory and synchronise before
+ * they return.  Entry points suffixed _dev take device pointers and are
+ * asynchronous on `stream`.
+ *
+ * Threading: there is no mutable global state except the default
+ * optimisation type set by sdg_dg_optr_kernel_setup, which mirrors the
+ * reference's module variable eval_typeid (mod_dg_optr_kernel.f90:36).
+ * A solver handle must be used by one host thread at a time.
+ */
+#ifndef SDG_ADVECT_H
+#define SDG_ADVECT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SDG_OK 0
+#define SDG_ERR_INVALID_ARG (-1)   /* bad size, NULL pointer, bad stage ... */
+#define SDG_ERR_UNSUPPORTED_ORDER (-2) /* PolyOrder outside 1..15 */
+#define SDG_ERR_BAD_OPTTYPE (-3)   /* not "GENERAL" / "OPT1", or never set */
+#define SDG_ERR_CUDA (-4)          /* a CUDA runtime call failed */
+#define SDG_ERR_OUT_OF_MEMORY (-5) /* device or host allocation failed */
+#define SDG_ERR_FILE (-6)          /* operator file missing or malformed */
+#define SDG_ERR_MESH (-7)          /* index out of range / not the mesh expected */
+#define SDG_ERR_TIMEOUT (-8)       /* a bounded wait expired */
+#define SDG_ERR_NO_DEVICE (-9)     /* no CUDA device is visible */
+
+/* DGOptrKernel optimisation types (mod_dg_optr_kernel.f90:38-42). */
+#define SDG_OPT_GENERAL 1
+#define SDG_OPT_OPT1 2
+
+/* Arithmetic of a solver (the reference is FP64 throughout). */
+#define SDG_PREC_FP64 0   /* FP64 state and FP64 arithmetic on the DFMA pipe */
+#define SDG_PREC_FP32 1   /* FP32 flux/derivative/lift, FP64 RK state */
+
+const char* sdg_status_string(int status);
+const char* sdg_last_error(void);
+/* Library version string. */
+const char* sdg_version(void);
+/* Number of visible CUDA devices (0 when none); never fails. */
+int sdg_device_count(void);
+/* Makes `device` current for the calling host thread (cudaSetDevice). */
+int sdg_set_device(int device);
+/* Blocks until all work on the current device has finished. */
+int sdg_device_synchronize(void);
+
+/* ---- DG operator data -------------------------------------------------- */
+
+/* Reads operator_data/p<p>.dat the way element_init does
+ * (mod_mesh.f90:253-263): x1D(Nq), D1D(Nq,Nq), Lift_mat(Nq,Nq,Nq,6), each
+ * starting on a new record; D1D_tr = transpose(D1D).  D1D_tr may be NULL. */
+int sdg_operator_read(const char* path, int p, double* x1D, double* D1D,
+                      double* D1D_tr, double* Lift_mat);
+
+/* Computes the same operators from the mathematics (Gauss-Lobatto-Legendre
+ * nodes, Lagrange differentiation matrix, lift = inverse 1-D mass matrix
+ * applied to the face node, identity across the face).  No counterpart in the
+ * reference, which loads them from files exported by FE-Project; the values
+ * agree with operator_data/p*.dat to rounding.  D1D_tr may be NULL. */
+int sdg_operator_generate(int p, double* x1D, double* D1D, double* D1D_tr,
+                          double* Lift_mat);
+
+/* ---- drop-in for mod_dg_optr_kernel / mod_advect3d_eq ------------------ */
+
+/* dg_optr_kernel_setup (mod_dg_optr_kernel.f90:45-58): "GENERAL" or "OPT1"
+ * (trailing blanks ignored, as trim() does).  Unlike the reference, an
+ * unknown string returns SDG_ERR_BAD_OPTTYPE and leaves the setting as it
+ * was. */
+int sdg_dg_optr_kernel_setup(const char* dgoptr_evaltype);
+/* The current default type (SDG_OPT_*), or 0 if never set. */
+int sdg_dg_optr_kernel_type(void);
+
+/* advect3d_eq_cal_tend (mod_advect3d_eq.f90:41-85), same argument list and
+ * meaning, host pointers.  q,u,v,w,dqdt are (Np,NeA) with halos filled by
+ * the caller (main.f90:59, :159-162); only dqdt(:,1:Ne) is written.  Uses the
+ * type set by sdg_dg_optr_kernel_setup.  Every VMap entry is range-checked
+ * on the device; an index outside 1..Np*NeA returns SDG_ERR_MESH. */
+int sdg_advect3d_eq_cal_tend(double* dqdt, const double* q, const double* u,
+                             const double* v, const double* w,
+                             const double* D1D, const double* D1D_tr,
+                             const double* Lift_mat, const int* VMapM,
+                             const int* VMapP, const double* normal_fn,
+                             const double* Escale, const double* Fscale,
+                             int Nq, int Np, int NfpTot, int Ne, int NeA);
+
+/* The same on device pointers, asynchronous on `stream`, with the
+ * optimisation type explicit.  `flux_scratch` is caller-owned device memory
+ * of NfpTot*Ne doubles for the element-boundary flux (the reference's
+ * automatic array ebnd_flux, mod_advect3d_eq.f90:66); `err_flag` is a
+ * caller-owned device int that the kernels set to 1 when a VMap index is out
+ * of range (it is not cleared here). */
+int sdg_advect3d_eq_cal_tend_dev(double* dqdt, const double* q,
+                                 const double* u, const double* v,
+                                 const double* w, const double* D1D,
+                                 const double* D1D_tr, const double* Lift_mat,
+                                 const int* VMapM, const int* VMapP,
+                                 const double* normal_fn,
+                                 const double* Escale, const double* Fscale,
+                                 int Nq, int Np, int NfpTot, int Ne, int NeA,
+                                 int opt, double* flux_scratch, int* err_flag,
+                                 void* stream);
+
+/* tensorprod_divlike_dirXYZ (mod_dg_optr_kernel.f90:62-136) over nelem
+ * consecutive elements (nelem = 1 is the reference call made per element from
+ * mod_advect3d_eq.f90:185-188).  Each array holds nelem blocks of Nq^3
+ * values.  Host pointers; uses the type set by sdg_dg_optr_kernel_setup. */
+int sdg_tensorprod_divlike_dirXYZ(double* vec_out_x, double* vec_out_y,
+                                  double* vec_out_z, const double* Mat,
+                                  const double* Mat_tr, const double* vec_in_x,
+                                  const double* vec_in_y,
+                                  const double* vec_in_z, int Nq, int nelem);
+int sdg_tensorprod_divlike_dirXYZ_dev(double* vec_out_x, double* vec_out_y,
+                                      double* vec_out_z, const double* Mat,
+                                      const double* Mat_tr,
+                                      const double* vec_in_x,
+                                      const double* vec_in_y,
+                                      const double* vec_in_z, int Nq,
+                                      int nelem, int opt, void* stream);
+
+/* tensorprod_Lift_hexahedral (mod_dg_optr_kernel.f90:139-190) over nelem
+ * elements: vec_in holds nelem blocks of (Nq,Nq,6), vec_out nelem blocks of
+ * Nq^3 values. */
+int sdg_tensorprod_Lift_hexahedral(double* vec_out, const double* Lift,
+                                   const double* vec_in, int Nq, int nelem);
+int sdg_tensorprod_Lift_hexahedral_dev(double* vec_out, const double* Lift,
+                                       const double* vec_in, int Nq, int nelem,
+                                       void* stream);
+
+/* update_halo (mod_mesh.f90:209-221) on a device field f(Np*NeA):
+ * f(Np*Ne+b) = f(halo_src_map(b)), b = 1..NhaloNode (1-based map).  A map
+ * entry outside the owned DOFs 1..Np*Ne (the only targets mesh_setup
+ * produces, mod_mesh.f90:184) is skipped rather than followed. */
+int sdg_update_halo_dev(double* f, const int* halo_src_map, int Np, int Ne,
+                        int NhaloNode, void* stream);
+
+/* RK stage combine of main.f90:68-73 on device arrays over the owned
+ * elements: q = rk_a(s)*q0 + rk_b(s)*(q + dt*dqdt), stage s = 1..3, with the
+ * SSP-RK3 coefficients of mod_common.f90:27-30. */
+int sdg_rk_stage_dev(double* q, const double* q0, const double* dqdt, int Np,
+                     int Ne, int stage, double dt, void* stream);
+
+/* ---- device-resident solver (replaces the time loop of main.f90:51-80) -- */
+
+/* A periodic structured box of NeX x NeY x NeZ hexahedra of order p on
+ * [0,Lx]x[0,Ly]x[0,Lz], exactly the mesh mesh_setup builds
+ * (mod_mesh.f90:74-193).  Neighbours are computed from the element index,
+ * so no VMap/normal/scale arrays and no halo buffer are stored, and the
+ * halo update disappears from the loop.  One step is three fused stage
+ * kernels (face flux + lift + divergence + RK combine), reading and writing
+ * rotating state buffers. */
+typedef struct sdg_solver sdg_solver;
+
+/* D1D(Nq,Nq) and Lift_mat(Nq,Nq,Nq,6) as read from operator_data (or from
+ * sdg_operator_generate).  opt = SDG_OPT_GENERAL / SDG_OPT_OPT1 selects the
+ * summation order of the divergence (they differ only for p > 7).
+ * precision = SDG_PREC_*.  stream may be NULL. */
+int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
+                      double Lx, double Ly, double Lz, const double* D1D,
+                      const double* Lift_mat, int opt, int precision,
+                      void* stream);
+/* Checks that caller-built mesh arrays (the reference's mesh_setup outputs,
+ * same shapes as in sdg_advect3d_eq_cal_tend) describe exactly the box this
+ * solver computes; returns SDG_ERR_MESH at the first difference. */
+int sdg_solver_check_mesh(const sdg_solver* s, const int* VMapM,
+                          const int* VMapP, const double* normal_fn,
+                          const double* Escale, const double* Fscale);
+/* Copies the owned part (Np*Ne values) of q,u,v,w from host memory. */
+int sdg_solver_upload(sdg_solver* s, const double* q, const double* u,
+                      const double* v, const double* w);
+/* The same from device memory (asynchronous on the solver's stream). */
+int sdg_solver_upload_dev(sdg_solver* s, const double* q, const double* u,
+                          const double* v, const double* w);
+/* Advances nstep SSP-RK3 steps of size dt (asynchronous). */
+int sdg_solver_step(sdg_solver* s, double dt, int nstep);
+/* sdg_solver_step bracketed by CUDA events on the solver's stream; waits
+ * for the end event and returns the elapsed device time in *ms. */
+int sdg_solver_step_timed(sdg_solver* s, double dt, int nstep, double* ms);
+/* Copies q (owned part, Np*Ne values) to host memory; synchronises. */
+int sdg_solver_download(sdg_solver* s, double* q);
+/* Device pointer of the current state q (Np*Ne doubles). */
+const double* sdg_solver_state_dev(const sdg_solver* s);
+/* Evaluates the tendency of the current state into dqdt (owned part,
+ * host memory), the fused-kernel analogue of advect3d_eq_cal_tend. */
+int sdg_solver_tendency(sdg_solver* s, double* dqdt);
+/* Kernel launches one step issues (for launch accounting). */
+int sdg_solver_launches_per_step(const sdg_solver* s);
+/* The solver's stream as void*. */
+void* sdg_solver_stream(const sdg_solver* s);
+int sdg_solver_destroy(sdg_solver* s);
+
+/* ---- measurement helpers ----------------------------------------------- */
+
+/* Device memory for callers of the *_dev entry points that have no CUDA
+ * runtime of their own (a Fortran or Python host). */
+int sdg_dev_alloc(size_t bytes, void** out);
+int sdg_dev_free(void* p);
+int sdg_memcpy_h2d(void* dst, const void* src, size_t bytes);
+int sdg_memcpy_d2h(void* dst, const void* src, size_t bytes);
+int sdg_memset_dev(void* dst, int value, size_t bytes);
+
+/* Page-locked host memory for fast host<->device copies (cudaHostAlloc). */
+int sdg_pinned_alloc(size_t bytes, void** out);
+int sdg_pinned_free(void* p);
+
+/* Peak-rate microbenchmark on the current device: dependent-chain-free
+ * DFMA, FFMA and FP64<->FP32 conversion throughput, in 1e12 operations per
+ * second (an FMA counts as 2 flops in the *_tflops results). */
+int sdg_microbench_peaks(double* dfma_tflops, double* ffma_tflops,
+                         double* cvt_f64_f32_tops, double* cvt_f32_f64_tops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

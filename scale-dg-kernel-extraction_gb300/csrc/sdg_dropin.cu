@@ -1,0 +1,342 @@
+// Reference-shaped entry points: advect3d_eq_cal_tend, the two DG operators,
+// update_halo and the RK combine, on host or device pointers.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "sdg_dropin.cuh"
+
+namespace sdg {
+
+#define SDG_DECL_DROPIN(p) \
+  int dropin_p##p(int what, int opt, const void* args, cudaStream_t st);
+SDG_DECL_DROPIN(1) SDG_DECL_DROPIN(2) SDG_DECL_DROPIN(3) SDG_DECL_DROPIN(4)
+SDG_DECL_DROPIN(5) SDG_DECL_DROPIN(6) SDG_DECL_DROPIN(7) SDG_DECL_DROPIN(8)
+SDG_DECL_DROPIN(9) SDG_DECL_DROPIN(10) SDG_DECL_DROPIN(11) SDG_DECL_DROPIN(12)
+SDG_DECL_DROPIN(13) SDG_DECL_DROPIN(14) SDG_DECL_DROPIN(15)
+#undef SDG_DECL_DROPIN
+
+// what: 0 = cal_dqdt, 1 = divlike, 2 = lift (mod_dg_optr_kernel.f90:87-133
+// and :155-186 select the per-order kernel the same way).
+static int dropin(int p, int what, int opt, const void* args, cudaStream_t st) {
+  switch (p) {
+    case 1: return dropin_p1(what, opt, args, st);
+    case 2: return dropin_p2(what, opt, args, st);
+    case 3: return dropin_p3(what, opt, args, st);
+    case 4: return dropin_p4(what, opt, args, st);
+    case 5: return dropin_p5(what, opt, args, st);
+    case 6: return dropin_p6(what, opt, args, st);
+    case 7: return dropin_p7(what, opt, args, st);
+    case 8: return dropin_p8(what, opt, args, st);
+    case 9: return dropin_p9(what, opt, args, st);
+    case 10: return dropin_p10(what, opt, args, st);
+    case 11: return dropin_p11(what, opt, args, st);
+    case 12: return dropin_p12(what, opt, args, st);
+    case 13: return dropin_p13(what, opt, args, st);
+    case 14: return dropin_p14(what, opt, args, st);
+    case 15: return dropin_p15(what, opt, args, st);
+    default: return fail(SDG_ERR_UNSUPPORTED_ORDER, "PolyOrder %d outside 1..15", p);
+  }
+}
+
+static int check_opt(int opt) {
+  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1)
+    return fail(SDG_ERR_BAD_OPTTYPE,
+                "DGOptrKernel type not set (call sdg_dg_optr_kernel_setup) or "
+                "unknown (%d)", opt);
+  return SDG_OK;
+}
+
+static int check_order(int Nq) {
+  if (Nq - 1 < 1 || Nq - 1 > kMaxOrder)
+    return fail(SDG_ERR_UNSUPPORTED_ORDER, "PolyOrder %d outside 1..15", Nq - 1);
+  return SDG_OK;
+}
+
+static int check_tend_shape(int Nq, int Np, int NfpTot, int Ne, int NeA) {
+  SDG_TRY(check_order(Nq));
+  if (Np != Nq * Nq * Nq || NfpTot != 6 * Nq * Nq || Ne < 0 || NeA < Ne)
+    return fail(SDG_ERR_INVALID_ARG,
+                "inconsistent sizes Nq=%d Np=%d NfpTot=%d Ne=%d NeA=%d", Nq, Np,
+                NfpTot, Ne, NeA);
+  return SDG_OK;
+}
+
+// One device allocation carved into aligned pieces; freed on scope exit.
+class Arena {
+ public:
+  ~Arena() {
+    if (base_) cudaFree(base_);
+  }
+  size_t add(size_t bytes) {
+    const size_t off = size_;
+    size_ += (bytes + 255) & ~size_t(255);
+    return off;
+  }
+  int alloc() {
+    if (size_ == 0) return SDG_OK;
+    SDG_CUDA_TRY(cudaMalloc(&base_, size_));
+    return SDG_OK;
+  }
+  template <typename T>
+  T* at(size_t off) const { return reinterpret_cast<T*>(static_cast<char*>(base_) + off); }
+
+ private:
+  void* base_ = nullptr;
+  size_t size_ = 0;
+};
+
+// cal_elembnd_flux, mod_advect3d_eq.f90:116-140, one thread per face node.
+__global__ void flux_kernel(const TendArgs a, int NfpTot) {
+  const long long NT = (long long)NfpTot * a.Ne;
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < NT;
+       m += (long long)gridDim.x * blockDim.x) {
+    const long long iM = (long long)a.VMapM[m] - 1, iP = (long long)a.VMapP[m] - 1;
+    if (iM < 0 || iM >= a.NpNeA || iP < 0 || iP >= a.NpNeA) {
+      atomicExch(a.err, 1);
+      a.flux[m] = 0.0;
+      continue;
+    }
+    const double n1 = a.normal_fn[m], n2 = a.normal_fn[m + NT],
+                 n3 = a.normal_fn[m + 2 * NT];
+    const double qM = a.q[iM], qP = a.q[iP];
+    const double VelM = a.u[iM] * n1 + a.v[iM] * n2 + a.w[iM] * n3;
+    const double VelP = a.u[iP] * n1 + a.v[iP] * n2 + a.w[iP] * n3;
+    const double alpha = 0.5 * fabs(VelP + VelM);
+    a.flux[m] = (0.5 * a.Fscale[m]) * ((qP * VelP - qM * VelM) - alpha * (qP - qM));
+  }
+}
+
+int tend_dev(const TendArgs& a, int p, int NfpTot, int opt, cudaStream_t st) {
+  if (a.Ne == 0) return SDG_OK;
+  const long long NT = (long long)NfpTot * a.Ne;
+  long long nb = (NT + 255) / 256;
+  if (nb > 152LL * 64) nb = 152LL * 64;
+  flux_kernel<<<(unsigned)nb, 256, 0, st>>>(a, NfpTot);
+  SDG_CUDA_TRY(cudaGetLastError());
+  return dropin(p, 0, opt, &a, st);
+}
+
+}  // namespace sdg
+
+using namespace sdg;
+
+namespace {
+
+__global__ void update_halo_kernel(double* f, const int* map, long long base,
+                                   long long nhalo, long long limit, int* err) {
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < nhalo;
+       b += (long long)gridDim.x * blockDim.x) {
+    const long long src = (long long)map[b] - 1;
+    if (src < 0 || src >= limit) {
+      if (err) atomicExch(err, 1);
+      continue;
+    }
+    f[base + b] = f[src];
+  }
+}
+
+__global__ void rk_kernel(double* q, const double* q0, const double* dqdt,
+                          long long n, double a, double b, double dt) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    // main.f90:70-71: rk_a*q0 + rk_b*(q + dt*dqdt)
+    const double r = b * (q[i] + dt * dqdt[i]);
+    q[i] = (a != 0.0) ? a * q0[i] + r : r;
+  }
+}
+
+unsigned grid_for(long long n) {
+  long long nb = (n + 255) / 256;
+  if (nb > 152LL * 64) nb = 152LL * 64;
+  return (unsigned)(nb > 0 ? nb : 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdg_advect3d_eq_cal_tend_dev(double* dqdt, const double* q, const double* u,
+                                 const double* v, const double* w,
+                                 const double* D1D, const double* D1D_tr,
+                                 const double* Lift_mat, const int* VMapM,
+                                 const int* VMapP, const double* normal_fn,
+                                 const double* Escale, const double* Fscale,
+                                 int Nq, int Np, int NfpTot, int Ne, int NeA,
+                                 int opt, double* flux_scratch, int* err_flag,
+                                 void* stream) {
+  SDG_TRY(check_opt(opt));
+  SDG_TRY(check_tend_shape(Nq, Np, NfpTot, Ne, NeA));
+  if (Ne == 0) return SDG_OK;
+  if (!dqdt || !q || !u || !v || !w || !D1D || !D1D_tr || !Lift_mat || !VMapM ||
+      !VMapP || !normal_fn || !Escale || !Fscale || !flux_scratch || !err_flag)
+    return fail(SDG_ERR_INVALID_ARG, "NULL device pointer");
+  TendArgs a{dqdt, q, u, v, w, D1D, D1D_tr, Lift_mat, VMapM, VMapP, normal_fn,
+             Escale, Fscale, flux_scratch, err_flag, Ne, (long long)Np * NeA};
+  return tend_dev(a, Nq - 1, NfpTot, opt, as_stream(stream));
+}
+
+int sdg_advect3d_eq_cal_tend(double* dqdt, const double* q, const double* u,
+                             const double* v, const double* w, const double* D1D,
+                             const double* D1D_tr, const double* Lift_mat,
+                             const int* VMapM, const int* VMapP,
+                             const double* normal_fn, const double* Escale,
+                             const double* Fscale, int Nq, int Np, int NfpTot,
+                             int Ne, int NeA) {
+  const int opt = sdg_dg_optr_kernel_type();
+  SDG_TRY(check_opt(opt));
+  SDG_TRY(check_tend_shape(Nq, Np, NfpTot, Ne, NeA));
+  if (Ne == 0) return SDG_OK;
+  if (!dqdt || !q || !u || !v || !w || !D1D || !D1D_tr || !Lift_mat || !VMapM ||
+      !VMapP || !normal_fn || !Escale || !Fscale)
+    return fail(SDG_ERR_INVALID_ARG, "NULL host pointer");
+  SDG_TRY(require_device());
+  const size_t nA = (size_t)Np * NeA, nO = (size_t)Np * Ne, nF = (size_t)NfpTot * Ne,
+               nD = (size_t)Nq * Nq, nL = 6 * (size_t)Np;
+  Arena ar;
+  const size_t oq = ar.add(8 * nA), ou = ar.add(8 * nA), ov = ar.add(8 * nA),
+               ow = ar.add(8 * nA), od = ar.add(8 * nO), oD = ar.add(8 * nD),
+               oDt = ar.add(8 * nD), oL = ar.add(8 * nL), oM = ar.add(4 * nF),
+               oP = ar.add(4 * nF), oN = ar.add(8 * 3 * nF), oE = ar.add(8 * 3 * nO),
+               oS = ar.add(8 * nF), oX = ar.add(8 * nF), oR = ar.add(sizeof(int));
+  SDG_TRY(ar.alloc());
+  cudaStream_t st = nullptr;
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(oq), q, 8 * nA, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(ou), u, 8 * nA, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(ov), v, 8 * nA, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(ow), w, 8 * nA, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(oD), D1D, 8 * nD, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(oDt), D1D_tr, 8 * nD, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(oL), Lift_mat, 8 * nL, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(oM), VMapM, 4 * nF, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(oP), VMapP, 4 * nF, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(oN), normal_fn, 8 * 3 * nF, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(oE), Escale, 8 * 3 * nO, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(ar.at<void>(oS), Fscale, 8 * nF, cudaMemcpyHostToDevice, st));
+  SDG_CUDA_TRY(cudaMemsetAsync(ar.at<void>(oR), 0, sizeof(int), st));
+  TendArgs a{ar.at<double>(od), ar.at<double>(oq), ar.at<double>(ou),
+             ar.at<double>(ov), ar.at<double>(ow), ar.at<double>(oD),
+             ar.at<double>(oDt), ar.at<double>(oL), ar.at<int>(oM),
+             ar.at<int>(oP), ar.at<double>(oN), ar.at<double>(oE),
+             ar.at<double>(oS), ar.at<double>(oX), ar.at<int>(oR), Ne,
+             (long long)Np * NeA};
+  SDG_TRY(tend_dev(a, Nq - 1, NfpTot, opt, st));
+  int err = 0;
+  SDG_CUDA_TRY(cudaMemcpyAsync(&err, ar.at<void>(oR), sizeof(int), cudaMemcpyDeviceToHost, st));
+  SDG_CUDA_TRY(cudaMemcpyAsync(dqdt, ar.at<void>(od), 8 * nO, cudaMemcpyDeviceToHost, st));
+  SDG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (err) return fail(SDG_ERR_MESH, "a VMapM/VMapP entry is outside 1..Np*NeA");
+  return SDG_OK;
+}
+
+int sdg_tensorprod_divlike_dirXYZ_dev(double* ox, double* oy, double* oz,
+                                      const double* Mat, const double* Mat_tr,
+                                      const double* ix, const double* iy,
+                                      const double* iz, int Nq, int nelem,
+                                      int opt, void* stream) {
+  SDG_TRY(check_opt(opt));
+  SDG_TRY(check_order(Nq));
+  if (nelem < 0) return fail(SDG_ERR_INVALID_ARG, "nelem < 0");
+  if (nelem == 0) return SDG_OK;
+  if (!ox || !oy || !oz || !Mat || !Mat_tr || !ix || !iy || !iz)
+    return fail(SDG_ERR_INVALID_ARG, "NULL device pointer");
+  DivArgs a{ox, oy, oz, Mat, Mat_tr, ix, iy, iz, nelem};
+  return dropin(Nq - 1, 1, opt, &a, as_stream(stream));
+}
+
+int sdg_tensorprod_divlike_dirXYZ(double* ox, double* oy, double* oz,
+                                  const double* Mat, const double* Mat_tr,
+                                  const double* ix, const double* iy,
+                                  const double* iz, int Nq, int nelem) {
+  const int opt = sdg_dg_optr_kernel_type();
+  SDG_TRY(check_opt(opt));
+  SDG_TRY(check_order(Nq));
+  if (nelem < 0) return fail(SDG_ERR_INVALID_ARG, "nelem < 0");
+  if (nelem == 0) return SDG_OK;
+  if (!ox || !oy || !oz || !Mat || !Mat_tr || !ix || !iy || !iz)
+    return fail(SDG_ERR_INVALID_ARG, "NULL host pointer");
+  SDG_TRY(require_device());
+  const size_t n = (size_t)Nq * Nq * Nq * nelem, nD = (size_t)Nq * Nq;
+  Arena ar;
+  const size_t o[8] = {ar.add(8 * n), ar.add(8 * n), ar.add(8 * n), ar.add(8 * nD),
+                       ar.add(8 * nD), ar.add(8 * n), ar.add(8 * n), ar.add(8 * n)};
+  SDG_TRY(ar.alloc());
+  const double* hin[5] = {Mat, Mat_tr, ix, iy, iz};
+  const size_t sz[5] = {nD, nD, n, n, n};
+  for (int t = 0; t < 5; t++)
+    SDG_CUDA_TRY(cudaMemcpy(ar.at<void>(o[3 + t]), hin[t], 8 * sz[t], cudaMemcpyHostToDevice));
+  DivArgs a{ar.at<double>(o[0]), ar.at<double>(o[1]), ar.at<double>(o[2]),
+            ar.at<double>(o[3]), ar.at<double>(o[4]), ar.at<double>(o[5]),
+            ar.at<double>(o[6]), ar.at<double>(o[7]), nelem};
+  SDG_TRY(dropin(Nq - 1, 1, opt, &a, nullptr));
+  SDG_CUDA_TRY(cudaMemcpy(ox, a.ox, 8 * n, cudaMemcpyDeviceToHost));
+  SDG_CUDA_TRY(cudaMemcpy(oy, a.oy, 8 * n, cudaMemcpyDeviceToHost));
+  SDG_CUDA_TRY(cudaMemcpy(oz, a.oz, 8 * n, cudaMemcpyDeviceToHost));
+  return SDG_OK;
+}
+
+int sdg_tensorprod_Lift_hexahedral_dev(double* out, const double* Lift,
+                                       const double* in, int Nq, int nelem,
+                                       void* stream) {
+  SDG_TRY(check_order(Nq));
+  if (nelem < 0) return fail(SDG_ERR_INVALID_ARG, "nelem < 0");
+  if (nelem == 0) return SDG_OK;
+  if (!out || !Lift || !in) return fail(SDG_ERR_INVALID_ARG, "NULL device pointer");
+  DivArgs a{out, nullptr, nullptr, Lift, nullptr, in, nullptr, nullptr, nelem};
+  return dropin(Nq - 1, 2, SDG_OPT_GENERAL, &a, as_stream(stream));
+}
+
+int sdg_tensorprod_Lift_hexahedral(double* out, const double* Lift,
+                                   const double* in, int Nq, int nelem) {
+  SDG_TRY(check_order(Nq));
+  if (nelem < 0) return fail(SDG_ERR_INVALID_ARG, "nelem < 0");
+  if (nelem == 0) return SDG_OK;
+  if (!out || !Lift || !in) return fail(SDG_ERR_INVALID_ARG, "NULL host pointer");
+  SDG_TRY(require_device());
+  const size_t np = (size_t)Nq * Nq * Nq;
+  const size_t n = np * nelem, nin = 6 * (size_t)Nq * Nq * nelem, nL = 6 * np;
+  Arena ar;
+  const size_t oo = ar.add(8 * n), oL = ar.add(8 * nL), oi = ar.add(8 * nin);
+  SDG_TRY(ar.alloc());
+  SDG_CUDA_TRY(cudaMemcpy(ar.at<void>(oL), Lift, 8 * nL, cudaMemcpyHostToDevice));
+  SDG_CUDA_TRY(cudaMemcpy(ar.at<void>(oi), in, 8 * nin, cudaMemcpyHostToDevice));
+  DivArgs a{ar.at<double>(oo), nullptr, nullptr, ar.at<double>(oL), nullptr,
+            ar.at<double>(oi), nullptr, nullptr, nelem};
+  SDG_TRY(dropin(Nq - 1, 2, SDG_OPT_GENERAL, &a, nullptr));
+  SDG_CUDA_TRY(cudaMemcpy(out, a.ox, 8 * n, cudaMemcpyDeviceToHost));
+  return SDG_OK;
+}
+
+int sdg_update_halo_dev(double* f, const int* halo_src_map, int Np, int Ne,
+                        int NhaloNode, void* stream) {
+  if (Np <= 0 || Ne < 0 || NhaloNode < 0)
+    return fail(SDG_ERR_INVALID_ARG, "bad sizes Np=%d Ne=%d NhaloNode=%d", Np, Ne,
+                NhaloNode);
+  if (NhaloNode == 0) return SDG_OK;
+  if (!f || !halo_src_map) return fail(SDG_ERR_INVALID_ARG, "NULL device pointer");
+  const long long base = (long long)Np * Ne;
+  // sources must be owned DOFs: 1..Np*Ne (mod_mesh.f90:184 only maps there)
+  update_halo_kernel<<<grid_for(NhaloNode), 256, 0, as_stream(stream)>>>(
+      f, halo_src_map, base, NhaloNode, base, nullptr);
+  SDG_CUDA_TRY(cudaGetLastError());
+  return SDG_OK;
+}
+
+int sdg_rk_stage_dev(double* q, const double* q0, const double* dqdt, int Np,
+                     int Ne, int stage, double dt, void* stream) {
+  // RK3 SSP coefficients, mod_common.f90:28-30
+  static const double rk_a[3] = {0.0, 0.75, 1.0 / 3.0};
+  static const double rk_b[3] = {1.0, 0.25, 2.0 / 3.0};
+  if (stage < 1 || stage > 3) return fail(SDG_ERR_INVALID_ARG, "stage %d outside 1..3", stage);
+  if (Np <= 0 || Ne < 0) return fail(SDG_ERR_INVALID_ARG, "bad sizes");
+  if (Ne == 0) return SDG_OK;
+  if (!q || !dqdt || (stage > 1 && !q0)) return fail(SDG_ERR_INVALID_ARG, "NULL device pointer");
+  const long long n = (long long)Np * Ne;
+  rk_kernel<<<grid_for(n), 256, 0, as_stream(stream)>>>(q, q0, dqdt, n, rk_a[stage - 1],
+                                                       rk_b[stage - 1], dt);
+  SDG_CUDA_TRY(cudaGetLastError());
+  return SDG_OK;
+}
+
+}  // extern "C"

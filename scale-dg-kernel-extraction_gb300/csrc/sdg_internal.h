@@ -1,0 +1,70 @@
+// Internal declarations shared by the translation units of libsdg_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+
+#include "sdg_advect.h"
+
+namespace sdg {
+
+constexpr int kMaxOrder = 15;
+
+// Records a message for sdg_last_error() (thread-local) and returns status.
+int fail(int status, const char* fmt, ...);
+// Maps a CUDA error to SDG_ERR_CUDA / SDG_ERR_OUT_OF_MEMORY with a message.
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define SDG_CUDA_TRY(call)                                              \
+  do {                                                                  \
+    cudaError_t sdg_e_ = (call);                                        \
+    if (sdg_e_ != cudaSuccess)                                          \
+      return ::sdg::cuda_fail(sdg_e_, #call, __FILE__, __LINE__);       \
+  } while (0)
+
+#define SDG_TRY(expr)                 \
+  do {                                \
+    int sdg_s_ = (expr);              \
+    if (sdg_s_ != SDG_OK) return sdg_s_; \
+  } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Checks the first CUDA device is usable; returns SDG_OK or an error status.
+int require_device();
+
+// Structured periodic box: what the fused stage kernel needs to know about the
+// mesh of mod_mesh.f90:74-193 (element order, per-axis scale factors).
+struct Box {
+  int NeX, NeY, NeZ;
+  long long Ne;
+  double Es[3];  // Escale(:,:,d) = 2/dx_d  (mod_mesh.f90:147-149)
+  double Fs[3];  // Fscale of the faces normal to axis d (mod_mesh.f90:366-394)
+};
+Box make_box(int NeX, int NeY, int NeZ, double Lx, double Ly, double Lz);
+
+// Arguments of one fused stage launch.
+struct StageArgs {
+  const double* q_in;   // state read by the stage (Np*Ne)
+  const double* q0;     // step-start state (stages 2 and 3), may be null if a==0
+  double* q_out;        // RK result (Np*Ne), or the tendency when tend_only
+  const void* u;        // velocity components (double or float, Np*Ne)
+  const void* v;
+  const void* w;
+  const void* D;        // D1D(Nq,Nq), column-major, compute type
+  const void* Lift;     // Lift_mat(Nq,Nq,Nq,6), compute type
+  Box box;
+  long long elem_begin;  // first element of this launch
+  long long elem_count;  // elements of this launch
+  double a, b, dt;      // q_out = a*q0 + b*(q_in + dt*dqdt)
+  int tend_only;        // write dqdt instead of the RK update
+};
+
+// Fused stage launchers (sdg_stage_*.cu).  prec = SDG_PREC_*.
+int launch_stage(int p, int prec, int opt, const StageArgs& a, cudaStream_t st);
+// Dynamic shared memory the launcher uses for order p, to size opt-in limits.
+int stage_setup_attributes(int p, int prec, int opt);
+
+}  // namespace sdg

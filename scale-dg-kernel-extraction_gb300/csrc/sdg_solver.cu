@@ -1,0 +1,319 @@
+// Device-resident solver for the periodic structured box: state, velocity and
+// operators live in HBM; a step is three fused stage launches over rotating
+// state buffers (the time loop of main.f90:51-80 without the q0 copy pass and
+// without update_halo).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "sdg_internal.h"
+
+using namespace sdg;
+
+struct sdg_solver {
+  int p = 0, Nq = 0, Np = 0, opt = 0, prec = 0;
+  Box box{};
+  long long ndof = 0;  // Np * Ne
+  cudaStream_t stream = nullptr;
+  double* q[3] = {nullptr, nullptr, nullptr};
+  int cur = 0;
+  void* u = nullptr;
+  void* v = nullptr;
+  void* w = nullptr;
+  void* D = nullptr;
+  void* Lift = nullptr;
+  double* dqdt = nullptr;
+};
+
+namespace {
+
+__global__ void f64_to_f32_kernel(float* out, const double* in, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+unsigned grid_for(long long n) {
+  long long nb = (n + 255) / 256;
+  if (nb > 152LL * 64) nb = 152LL * 64;
+  return (unsigned)(nb > 0 ? nb : 1);
+}
+
+void release(sdg_solver* s) {
+  for (int i = 0; i < 3; i++) cudaFree(s->q[i]);
+  cudaFree(s->u);
+  cudaFree(s->v);
+  cudaFree(s->w);
+  cudaFree(s->D);
+  cudaFree(s->Lift);
+  cudaFree(s->dqdt);
+}
+
+int one_stage(sdg_solver* s, int stage, double dt, const double* qin,
+              const double* q0, double* qout, bool tend_only) {
+  static const double rk_a[3] = {0.0, 0.75, 1.0 / 3.0};  // mod_common.f90:28-30
+  static const double rk_b[3] = {1.0, 0.25, 2.0 / 3.0};
+  StageArgs a{};
+  a.q_in = qin;
+  a.q0 = q0;
+  a.q_out = qout;
+  a.u = s->u;
+  a.v = s->v;
+  a.w = s->w;
+  a.D = s->D;
+  a.Lift = s->Lift;
+  a.box = s->box;
+  a.elem_begin = 0;
+  a.elem_count = s->box.Ne;
+  a.a = rk_a[stage];
+  a.b = rk_b[stage];
+  a.dt = dt;
+  a.tend_only = tend_only ? 1 : 0;
+  return launch_stage(s->p, s->prec, s->opt, a, s->stream);
+}
+
+// Uploads one velocity component (device source) in the compute type.
+int put_velocity(sdg_solver* s, void* dst, const double* src_dev) {
+  const long long n = s->ndof;
+  if (s->prec == SDG_PREC_FP64) {
+    SDG_CUDA_TRY(cudaMemcpyAsync(dst, src_dev, 8 * (size_t)n, cudaMemcpyDeviceToDevice,
+                                 s->stream));
+  } else {
+    f64_to_f32_kernel<<<grid_for(n), 256, 0, s->stream>>>(static_cast<float*>(dst),
+                                                         src_dev, n);
+    SDG_CUDA_TRY(cudaGetLastError());
+  }
+  return SDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
+                      double Lx, double Ly, double Lz, const double* D1D,
+                      const double* Lift_mat, int opt, int precision,
+                      void* stream) {
+  if (!out) return fail(SDG_ERR_INVALID_ARG, "NULL output handle");
+  *out = nullptr;
+  if (p < 1 || p > kMaxOrder)
+    return fail(SDG_ERR_UNSUPPORTED_ORDER, "PolyOrder %d outside 1..15", p);
+  if (NeX < 1 || NeY < 1 || NeZ < 1 || !(Lx > 0) || !(Ly > 0) || !(Lz > 0))
+    return fail(SDG_ERR_INVALID_ARG, "bad box %dx%dx%d (%g,%g,%g)", NeX, NeY, NeZ,
+                Lx, Ly, Lz);
+  if ((long long)NeX * NeY * NeZ > 0x7fffffffLL)
+    return fail(SDG_ERR_INVALID_ARG, "too many elements");
+  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1)
+    return fail(SDG_ERR_BAD_OPTTYPE, "unknown DGOptrKernel type %d", opt);
+  if (precision != SDG_PREC_FP64 && precision != SDG_PREC_FP32)
+    return fail(SDG_ERR_INVALID_ARG, "unknown precision %d", precision);
+  if (!D1D || !Lift_mat) return fail(SDG_ERR_INVALID_ARG, "NULL operator");
+  SDG_TRY(require_device());
+  sdg_solver* s = new (std::nothrow) sdg_solver();
+  if (!s) return fail(SDG_ERR_OUT_OF_MEMORY, "host allocation failed");
+  s->p = p;
+  s->Nq = p + 1;
+  s->Np = s->Nq * s->Nq * s->Nq;
+  s->opt = opt;
+  s->prec = precision;
+  s->box = make_box(NeX, NeY, NeZ, Lx, Ly, Lz);
+  s->ndof = (long long)s->Np * s->box.Ne;
+  s->stream = as_stream(stream);
+  const size_t es = (precision == SDG_PREC_FP64) ? 8 : 4;
+  const size_t nD = (size_t)s->Nq * s->Nq, nL = 6 * (size_t)s->Np;
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 3 && e == cudaSuccess; i++)
+    e = cudaMalloc(&s->q[i], 8 * (size_t)s->ndof);
+  if (e == cudaSuccess) e = cudaMalloc(&s->u, es * (size_t)s->ndof);
+  if (e == cudaSuccess) e = cudaMalloc(&s->v, es * (size_t)s->ndof);
+  if (e == cudaSuccess) e = cudaMalloc(&s->w, es * (size_t)s->ndof);
+  if (e == cudaSuccess) e = cudaMalloc(&s->D, es * nD);
+  if (e == cudaSuccess) e = cudaMalloc(&s->Lift, es * nL);
+  if (e == cudaSuccess) {
+    if (precision == SDG_PREC_FP64) {
+      e = cudaMemcpy(s->D, D1D, 8 * nD, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(s->Lift, Lift_mat, 8 * nL, cudaMemcpyHostToDevice);
+    } else {
+      std::vector<float> dF(nD), lF(nL);
+      for (size_t i = 0; i < nD; i++) dF[i] = (float)D1D[i];
+      for (size_t i = 0; i < nL; i++) lF[i] = (float)Lift_mat[i];
+      e = cudaMemcpy(s->D, dF.data(), 4 * nD, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(s->Lift, lF.data(), 4 * nL, cudaMemcpyHostToDevice);
+    }
+  }
+  if (e != cudaSuccess) {
+    const int st = cuda_fail(e, "solver allocation", __FILE__, __LINE__);
+    release(s);
+    delete s;
+    return st;
+  }
+  *out = s;
+  return SDG_OK;
+}
+
+int sdg_solver_check_mesh(const sdg_solver* s, const int* VMapM, const int* VMapP,
+                          const double* normal_fn, const double* Escale,
+                          const double* Fscale) {
+  if (!s || !VMapM || !VMapP || !normal_fn || !Escale || !Fscale)
+    return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  // Rebuild mesh_setup's arrays element by element (mod_mesh.f90:132-190) and
+  // compare.  VMapP of a periodic boundary face points at a halo slot; the
+  // slot order is the serial loop of mod_mesh.f90:171-190, so it is replayed.
+  const int Nq = s->Nq, Np = s->Np, Nfp = Nq * Nq, NfpTot = 6 * Nfp;
+  const int NeX = s->box.NeX, NeY = s->box.NeY, NeZ = s->box.NeZ;
+  const long long Ne = s->box.Ne, NT = (long long)NfpTot * Ne, NpNe = (long long)Np * Ne;
+  const int naxis[6] = {1, 0, 1, 0, 2, 2};
+  const double nsign[6] = {-1, 1, 1, -1, -1, 1};
+  long long ibuf = 0;
+  for (int k = 0; k < NeZ; k++)
+    for (int j = 0; j < NeY; j++)
+      for (int i = 0; i < NeX; i++) {
+        const long long e = i + (long long)NeX * (j + (long long)NeY * k);
+        for (int n = 0; n < Np; n++)
+          for (int d = 0; d < 3; d++)
+            if (Escale[e * Np + n + d * NpNe] != s->box.Es[d])
+              return fail(SDG_ERR_MESH, "Escale differs at element %lld node %d", e + 1, n + 1);
+        for (int f = 0; f < 6; f++) {
+          int ni = i, nj = j, nk = k;
+          bool bnd = false;
+          switch (f) {
+            case 0: bnd = (j == 0); nj = bnd ? NeY - 1 : j - 1; break;
+            case 1: bnd = (i == NeX - 1); ni = bnd ? 0 : i + 1; break;
+            case 2: bnd = (j == NeY - 1); nj = bnd ? 0 : j + 1; break;
+            case 3: bnd = (i == 0); ni = bnd ? NeX - 1 : i - 1; break;
+            case 4: bnd = (k == 0); nk = bnd ? NeZ - 1 : k - 1; break;
+            default: bnd = (k == NeZ - 1); nk = bnd ? 0 : k + 1; break;
+          }
+          const long long eP = ni + (long long)NeX * (nj + (long long)NeY * nk);
+          for (int fp = 0; fp < Nfp; fp++) {
+            const int ta = fp % Nq, tb = fp / Nq, L = Nq - 1, Q2 = Nq * Nq;
+            int nM = 0, nP = 0;
+            switch (f) {
+              case 0: nM = ta + tb * Q2; nP = ta + L * Nq + tb * Q2; break;
+              case 1: nM = L + ta * Nq + tb * Q2; nP = ta * Nq + tb * Q2; break;
+              case 2: nM = ta + L * Nq + tb * Q2; nP = ta + tb * Q2; break;
+              case 3: nM = ta * Nq + tb * Q2; nP = L + ta * Nq + tb * Q2; break;
+              case 4: nM = ta + tb * Nq; nP = ta + tb * Nq + L * Q2; break;
+              default: nM = ta + tb * Nq + L * Q2; nP = ta + tb * Nq; break;
+            }
+            const long long m = e * NfpTot + f * Nfp + fp;
+            if (VMapM[m] != e * Np + nM + 1)
+              return fail(SDG_ERR_MESH, "VMapM differs at face node %lld", m + 1);
+            const long long want = bnd ? NpNe + (++ibuf) : eP * Np + nP + 1;
+            if (VMapP[m] != want)
+              return fail(SDG_ERR_MESH, "VMapP differs at face node %lld", m + 1);
+            for (int d = 0; d < 3; d++)
+              if (normal_fn[m + d * NT] != (d == naxis[f] ? nsign[f] : 0.0))
+                return fail(SDG_ERR_MESH, "normal_fn differs at face node %lld", m + 1);
+            if (Fscale[m] != s->box.Fs[naxis[f]])
+              return fail(SDG_ERR_MESH, "Fscale differs at face node %lld", m + 1);
+          }
+        }
+      }
+  return SDG_OK;
+}
+
+int sdg_solver_upload_dev(sdg_solver* s, const double* q, const double* u,
+                          const double* v, const double* w) {
+  if (!s || !q || !u || !v || !w) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  SDG_CUDA_TRY(cudaMemcpyAsync(s->q[s->cur], q, 8 * (size_t)s->ndof,
+                               cudaMemcpyDeviceToDevice, s->stream));
+  SDG_TRY(put_velocity(s, s->u, u));
+  SDG_TRY(put_velocity(s, s->v, v));
+  SDG_TRY(put_velocity(s, s->w, w));
+  return SDG_OK;
+}
+
+int sdg_solver_upload(sdg_solver* s, const double* q, const double* u,
+                      const double* v, const double* w) {
+  if (!s || !q || !u || !v || !w) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  const size_t bytes = 8 * (size_t)s->ndof;
+  SDG_CUDA_TRY(cudaMemcpyAsync(s->q[s->cur], q, bytes, cudaMemcpyHostToDevice, s->stream));
+  if (s->prec == SDG_PREC_FP64) {
+    SDG_CUDA_TRY(cudaMemcpyAsync(s->u, u, bytes, cudaMemcpyHostToDevice, s->stream));
+    SDG_CUDA_TRY(cudaMemcpyAsync(s->v, v, bytes, cudaMemcpyHostToDevice, s->stream));
+    SDG_CUDA_TRY(cudaMemcpyAsync(s->w, w, bytes, cudaMemcpyHostToDevice, s->stream));
+  } else {
+    // stage each FP64 component through a free state buffer, then narrow it
+    double* tmp = s->q[(s->cur + 1) % 3];
+    const double* src[3] = {u, v, w};
+    void* dst[3] = {s->u, s->v, s->w};
+    for (int c = 0; c < 3; c++) {
+      SDG_CUDA_TRY(cudaMemcpyAsync(tmp, src[c], bytes, cudaMemcpyHostToDevice, s->stream));
+      SDG_TRY(put_velocity(s, dst[c], tmp));
+    }
+  }
+  return SDG_OK;
+}
+
+int sdg_solver_step(sdg_solver* s, double dt, int nstep) {
+  if (!s) return fail(SDG_ERR_INVALID_ARG, "NULL solver");
+  if (nstep < 0) return fail(SDG_ERR_INVALID_ARG, "nstep < 0");
+  for (int it = 0; it < nstep; it++) {
+    const int s0 = s->cur, s1 = (s->cur + 1) % 3, s2 = (s->cur + 2) % 3;
+    SDG_TRY(one_stage(s, 0, dt, s->q[s0], nullptr, s->q[s1], false));
+    SDG_TRY(one_stage(s, 1, dt, s->q[s1], s->q[s0], s->q[s2], false));
+    SDG_TRY(one_stage(s, 2, dt, s->q[s2], s->q[s0], s->q[s1], false));
+    s->cur = s1;
+  }
+  return SDG_OK;
+}
+
+int sdg_solver_step_timed(sdg_solver* s, double dt, int nstep, double* ms) {
+  if (!s || !ms) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  SDG_CUDA_TRY(cudaEventCreate(&e0));
+  cudaError_t ce = cudaEventCreate(&e1);
+  if (ce != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return cuda_fail(ce, "cudaEventCreate", __FILE__, __LINE__);
+  }
+  int st = SDG_OK;
+  ce = cudaEventRecord(e0, s->stream);
+  if (ce == cudaSuccess) st = sdg_solver_step(s, dt, nstep);
+  if (ce == cudaSuccess && st == SDG_OK) ce = cudaEventRecord(e1, s->stream);
+  if (ce == cudaSuccess && st == SDG_OK) ce = cudaEventSynchronize(e1);
+  float f = 0.f;
+  if (ce == cudaSuccess && st == SDG_OK) ce = cudaEventElapsedTime(&f, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ce != cudaSuccess) return cuda_fail(ce, "solver timing", __FILE__, __LINE__);
+  if (st != SDG_OK) return st;
+  *ms = f;
+  return SDG_OK;
+}
+
+int sdg_solver_tendency(sdg_solver* s, double* dqdt) {
+  if (!s || !dqdt) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  if (!s->dqdt) SDG_CUDA_TRY(cudaMalloc(&s->dqdt, 8 * (size_t)s->ndof));
+  SDG_TRY(one_stage(s, 0, 0.0, s->q[s->cur], nullptr, s->dqdt, true));
+  SDG_CUDA_TRY(cudaMemcpyAsync(dqdt, s->dqdt, 8 * (size_t)s->ndof, cudaMemcpyDeviceToHost,
+                               s->stream));
+  SDG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return SDG_OK;
+}
+
+int sdg_solver_download(sdg_solver* s, double* q) {
+  if (!s || !q) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  SDG_CUDA_TRY(cudaMemcpyAsync(q, s->q[s->cur], 8 * (size_t)s->ndof,
+                               cudaMemcpyDeviceToHost, s->stream));
+  SDG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return SDG_OK;
+}
+
+const double* sdg_solver_state_dev(const sdg_solver* s) { return s ? s->q[s->cur] : nullptr; }
+
+int sdg_solver_launches_per_step(const sdg_solver* s) { return s ? 3 : 0; }
+
+void* sdg_solver_stream(const sdg_solver* s) { return s ? (void*)s->stream : nullptr; }
+
+int sdg_solver_destroy(sdg_solver* s) {
+  if (!s) return SDG_OK;
+  release(s);
+  delete s;
+  return SDG_OK;
+}
+
+}  // extern "C"

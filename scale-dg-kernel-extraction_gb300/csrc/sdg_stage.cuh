@@ -1,0 +1,269 @@
+// Fused RK-stage kernel for the periodic structured box.
+//
+// One launch advances every element of the box through one SSP-RK3 stage,
+// replacing, per stage, the reference's update_halo (mod_mesh.f90:209-221),
+// advect3d_eq_cal_tend (mod_advect3d_eq.f90:41-85: cal_elembnd_flux :89-142
+// and cal_dqdt :146-201 with the DG operators of mod_dg_optr_kernel.f90) and
+// the RK combine of main.f90:68-73.  A block owns EPB consecutive elements:
+//
+//   phase 0  stage q,u,v,w of its elements (contiguous, coalesced) and D1D
+//            in shared memory;
+//   phase 1  upwind flux on all 6*Nfp face nodes of each element: the minus
+//            side comes from shared memory, the plus side is gathered from
+//            the neighbour element's opposite face (computed from the
+//            element index with periodic wrap, which is what VMapP plus the
+//            halo buffer encode);
+//   phase 2  F_d = q*u_d in place;
+//   phase 3  per node: sum-factorised Dx/Dy/Dz contractions, the lift of the
+//            face fluxes, dqdt = -(Es_x Dx + Es_y Dy + Es_z Dz + Lift) and
+//            q_out = a*q0 + b*(q + dt*dqdt).
+//
+// The stage reads q_in and q0 and writes q_out, three distinct buffers, so a
+// block never overwrites what another block still gathers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sdg_internal.h"
+
+namespace sdg {
+
+template <int P>
+struct Ord {
+  static constexpr int NQ = P + 1;
+  static constexpr int NQ2 = NQ * NQ;
+  static constexpr int NP = NQ * NQ2;
+  static constexpr int NFP = NQ2;
+  static constexpr int NFT = 6 * NFP;
+};
+
+// Elements per block and threads per block of the fused stage kernel.
+template <int P, typename CT>
+struct StageCfg {
+  static constexpr int EPB = (P == 1) ? 32 : (P == 2) ? 16 : (P == 3) ? 8
+                           : (P == 4) ? 4 : (P <= 6) ? 2 : 1;
+  static constexpr int THREADS = (P >= 10) ? 512 : 256;
+};
+
+// sum_l Dcol[l*DS] * f[l*stride], l = 0..NQ-1.  GENERAL order: running sum
+// from zero (mod_dg_optr_kernel.f90:216-256).  OPT1 for p > 7: three partial
+// sums of round(NQ/3), round(NQ/3) and the rest, added as (t1+t2)+t3
+// (mod_dg_optr_kernel_opt1.F90.erb:42-44, :257-273).  DS is the stride of the
+// matrix entries: NQ for a row of D1D(i,:), 1 for a column of D1D_tr(:,j).
+template <int NQ, bool SPLIT3, int DS, typename T>
+__device__ __forceinline__ T line_sum(const T* __restrict__ Dcol,
+                                      const T* __restrict__ f, int stride) {
+  if constexpr (!SPLIT3) {
+    T s = Dcol[0] * f[0];
+#pragma unroll
+    for (int l = 1; l < NQ; l++) s = fma(Dcol[l * DS], f[l * stride], s);
+    return s;
+  } else {
+    constexpr int D3 = (2 * NQ + 3) / 6;  // round(NQ/3.0) for NQ in 9..16
+    T t1 = Dcol[0] * f[0];
+#pragma unroll
+    for (int l = 1; l < D3; l++) t1 = fma(Dcol[l * DS], f[l * stride], t1);
+    T t2 = Dcol[D3 * DS] * f[D3 * stride];
+#pragma unroll
+    for (int l = D3 + 1; l < 2 * D3; l++) t2 = fma(Dcol[l * DS], f[l * stride], t2);
+    T t3 = Dcol[2 * D3 * DS] * f[2 * D3 * stride];
+#pragma unroll
+    for (int l = 2 * D3 + 1; l < NQ; l++) t3 = fma(Dcol[l * DS], f[l * stride], t3);
+    return (t1 + t2) + t3;
+  }
+}
+
+// Lift of one node (mod_dg_optr_kernel.f90:274-286), faces in order 1..6.
+// L points at Lift_mat(n,1) (face stride NP); fl at the element's 6*NFP fluxes.
+template <int P, typename T>
+__device__ __forceinline__ T lift_node(const T* __restrict__ L,
+                                       const T* __restrict__ fl, int i, int j,
+                                       int k) {
+  using O = Ord<P>;
+  T s = __ldg(L) * fl[i + k * O::NQ];
+  s = fma(__ldg(L + 1 * O::NP), fl[1 * O::NFP + j + k * O::NQ], s);
+  s = fma(__ldg(L + 2 * O::NP), fl[2 * O::NFP + i + k * O::NQ], s);
+  s = fma(__ldg(L + 3 * O::NP), fl[3 * O::NFP + j + k * O::NQ], s);
+  s = fma(__ldg(L + 4 * O::NP), fl[4 * O::NFP + i + j * O::NQ], s);
+  s = fma(__ldg(L + 5 * O::NP), fl[5 * O::NFP + i + j * O::NQ], s);
+  return s;
+}
+
+// Face geometry of the structured element (mod_mesh.f90:265-324, :356-397):
+// for face f (0-based: -y,+x,+y,-x,-z,+z) and tangential indices (ta, tb),
+// the node on this face, the node with the same tangential indices on the
+// opposite face, the normal axis and sign.
+template <int NQ>
+__device__ __forceinline__ void face_nodes(int f, int ta, int tb, int& nM,
+                                           int& nP, int& axis, int& sgn) {
+  constexpr int NQ2 = NQ * NQ, L = NQ - 1;
+  switch (f) {
+    case 0: nM = ta + tb * NQ2;              nP = ta + L * NQ + tb * NQ2;  axis = 1; sgn = -1; break;
+    case 1: nM = L + ta * NQ + tb * NQ2;     nP = ta * NQ + tb * NQ2;      axis = 0; sgn = 1;  break;
+    case 2: nM = ta + L * NQ + tb * NQ2;     nP = ta + tb * NQ2;           axis = 1; sgn = 1;  break;
+    case 3: nM = ta * NQ + tb * NQ2;         nP = L + ta * NQ + tb * NQ2;  axis = 0; sgn = -1; break;
+    case 4: nM = ta + tb * NQ;               nP = ta + tb * NQ + L * NQ2;  axis = 2; sgn = -1; break;
+    default: nM = ta + tb * NQ + L * NQ2;    nP = ta + tb * NQ;            axis = 2; sgn = 1;  break;
+  }
+}
+
+// Neighbour across face f with periodic wrap (eval_neighbor_element,
+// mod_mesh.f90:407-483); element index e = ex + ey*NeX + ez*NeX*NeY.
+__device__ __forceinline__ long long neighbor(const Box& b, long long e, int f) {
+  const int NeX = b.NeX, NeY = b.NeY, NeZ = b.NeZ;
+  int ex = (int)(e % NeX);
+  long long r = e / NeX;
+  int ey = (int)(r % NeY);
+  int ez = (int)(r / NeY);
+  switch (f) {
+    case 0: ey = (ey == 0) ? NeY - 1 : ey - 1; break;
+    case 1: ex = (ex == NeX - 1) ? 0 : ex + 1; break;
+    case 2: ey = (ey == NeY - 1) ? 0 : ey + 1; break;
+    case 3: ex = (ex == 0) ? NeX - 1 : ex - 1; break;
+    case 4: ez = (ez == 0) ? NeZ - 1 : ez - 1; break;
+    default: ez = (ez == NeZ - 1) ? 0 : ez + 1; break;
+  }
+  return (long long)ex + (long long)NeX * (ey + (long long)NeY * ez);
+}
+
+template <typename T> __device__ __forceinline__ T to_ct(double x) { return (T)x; }
+template <typename T> __device__ __forceinline__ T to_ct(float x) { return (T)x; }
+
+template <int P, typename CT, typename VT, bool SPLIT3>
+constexpr size_t stage_smem_bytes() {
+  using O = Ord<P>;
+  using C = StageCfg<P, CT>;
+  return sizeof(CT) * (size_t)(O::NQ2 + C::EPB * (4 * O::NP + O::NFT));
+}
+
+template <int P, typename CT, typename VT, bool SPLIT3>
+__global__ void __launch_bounds__(StageCfg<P, CT>::THREADS)
+    stage_kernel(const StageArgs a) {
+  using O = Ord<P>;
+  using C = StageCfg<P, CT>;
+  constexpr int NQ = O::NQ, NQ2 = O::NQ2, NP = O::NP, NFP = O::NFP,
+                NFT = O::NFT, EPB = C::EPB, T = C::THREADS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CT* sD = reinterpret_cast<CT*>(smem_raw);
+  CT* sq = sD + NQ2;
+  CT* su = sq + EPB * NP;
+  CT* sv = su + EPB * NP;
+  CT* sw = sv + EPB * NP;
+  CT* sf = sw + EPB * NP;
+
+  const long long eb = a.elem_begin + (long long)blockIdx.x * EPB;
+  const long long eend = a.elem_begin + a.elem_count;
+  const int nloc = (int)((eend - eb) < EPB ? (eend - eb) : EPB);
+  if (nloc <= 0) return;
+  const double* __restrict__ qin = a.q_in;
+  const VT* __restrict__ gu = static_cast<const VT*>(a.u);
+  const VT* __restrict__ gv = static_cast<const VT*>(a.v);
+  const VT* __restrict__ gw = static_cast<const VT*>(a.w);
+  const long long g0 = eb * NP;
+
+  // phase 0: stage the block's elements
+  for (int t = threadIdx.x; t < NQ2; t += T) sD[t] = static_cast<const CT*>(a.D)[t];
+  for (int t = threadIdx.x; t < nloc * NP; t += T) {
+    sq[t] = to_ct<CT>(qin[g0 + t]);
+    su[t] = to_ct<CT>(gu[g0 + t]);
+    sv[t] = to_ct<CT>(gv[g0 + t]);
+    sw[t] = to_ct<CT>(gw[g0 + t]);
+  }
+  __syncthreads();
+
+  // phase 1: element-boundary flux (mod_advect3d_eq.f90:116-140)
+  for (int t = threadIdx.x; t < nloc * NFT; t += T) {
+    const int le = t / NFT;
+    const int r = t - le * NFT;
+    const int f = r / NFP;
+    const int fp = r - f * NFP;
+    int nM, nP, axis, sg;
+    face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sg);
+    const long long eP = neighbor(a.box, eb + le, f);
+    const CT* svel = (axis == 0) ? su : (axis == 1) ? sv : sw;
+    const VT* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
+    const long long gP = eP * NP + nP;
+    // normal velocity u.n with an axis-aligned unit normal is +-u_axis exactly
+    const CT sgn = (CT)sg;
+    const CT qM = sq[le * NP + nM];
+    const CT velM = sgn * svel[le * NP + nM];
+    const CT qP = to_ct<CT>(qin[gP]);
+    const CT velP = sgn * to_ct<CT>(gvel[gP]);
+    const CT alpha = CT(0.5) * fabs(velP + velM);
+    const CT fs = (CT)a.box.Fs[axis];
+    sf[le * NFT + r] = (CT(0.5) * fs) * ((qP * velP - qM * velM) - alpha * (qP - qM));
+  }
+  __syncthreads();
+
+  // phase 2: volume fluxes F_d = q * u_d (mod_advect3d_eq.f90:181-183)
+  for (int t = threadIdx.x; t < nloc * NP; t += T) {
+    const CT qq = sq[t];
+    su[t] = qq * su[t];
+    sv[t] = qq * sv[t];
+    sw[t] = qq * sw[t];
+  }
+  __syncthreads();
+
+  // phase 3: divergence + lift + combine + RK (mod_advect3d_eq.f90:185-198,
+  // main.f90:69-73)
+  const CT Ex = (CT)a.box.Es[0], Ey = (CT)a.box.Es[1], Ez = (CT)a.box.Es[2];
+  const CT* __restrict__ L = static_cast<const CT*>(a.Lift);
+  for (int t = threadIdx.x; t < nloc * NP; t += T) {
+    const int le = t / NP;
+    const int n = t - le * NP;
+    const int i = n % NQ;
+    const int j = (n / NQ) % NQ;
+    const int k = n / NQ2;
+    const CT* Fx = su + le * NP;
+    const CT* Fy = sv + le * NP;
+    const CT* Fz = sw + le * NP;
+    const CT dx = line_sum<NQ, SPLIT3, NQ>(sD + i, Fx + j * NQ + k * NQ2, 1);
+    const CT dy = line_sum<NQ, SPLIT3, NQ>(sD + j, Fy + i + k * NQ2, NQ);
+    const CT dz = line_sum<NQ, SPLIT3, NQ>(sD + k, Fz + i + j * NQ, NQ2);
+    const CT lf = lift_node<P>(L + n, sf + le * NFT, i, j, k);
+    const CT dq = -(((Ex * dx + Ey * dy) + Ez * dz) + lf);
+    const long long g = g0 + t;
+    if (a.tend_only) {
+      a.q_out[g] = (double)dq;
+    } else {
+      const double qv = qin[g];
+      double r = a.b * (qv + a.dt * (double)dq);
+      if (a.a != 0.0) r = a.a * a.q0[g] + r;
+      a.q_out[g] = r;
+    }
+  }
+}
+
+template <int P, typename CT, typename VT, bool SPLIT3>
+int launch_stage_impl(const StageArgs& a, cudaStream_t st) {
+  using C = StageCfg<P, CT>;
+  constexpr size_t smem = stage_smem_bytes<P, CT, VT, SPLIT3>();
+  static bool attr_done = false;
+  if (!attr_done) {
+    SDG_CUDA_TRY(cudaFuncSetAttribute(stage_kernel<P, CT, VT, SPLIT3>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    attr_done = true;
+  }
+  const long long nblk = (a.elem_count + C::EPB - 1) / C::EPB;
+  if (nblk <= 0) return SDG_OK;
+  if (nblk > 0x7fffffffLL) return fail(SDG_ERR_INVALID_ARG, "too many elements");
+  stage_kernel<P, CT, VT, SPLIT3><<<(unsigned)nblk, C::THREADS, smem, st>>>(a);
+  SDG_CUDA_TRY(cudaGetLastError());
+  return SDG_OK;
+}
+
+// Launches order P with the precision/optimisation choice resolved.
+template <int P>
+int launch_stage_order(int prec, int opt, const StageArgs& a, cudaStream_t st) {
+  constexpr bool kCanSplit = (P > 7);
+  const bool split = kCanSplit && (opt == SDG_OPT_OPT1);
+  if (prec == SDG_PREC_FP64) {
+    if (split) return launch_stage_impl<P, double, double, kCanSplit>(a, st);
+    return launch_stage_impl<P, double, double, false>(a, st);
+  }
+  if (split) return launch_stage_impl<P, float, float, kCanSplit>(a, st);
+  return launch_stage_impl<P, float, float, false>(a, st);
+}
+
+}  // namespace sdg

@@ -1,0 +1,9 @@
+// Instantiations of the fused stage kernel for orders 7 (one translation
+// unit per group so that the build compiles them in parallel).
+#include "sdg_stage.cuh"
+
+namespace sdg {
+int launch_stage_p7(int prec, int opt, const StageArgs& a, cudaStream_t st) {
+  return launch_stage_order<7>(prec, opt, a, st);
+}
+}  // namespace sdg

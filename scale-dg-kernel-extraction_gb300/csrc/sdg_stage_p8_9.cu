@@ -1,0 +1,12 @@
+// Instantiations of the fused stage kernel for orders 8 9 (one translation
+// unit per group so that the build compiles them in parallel).
+#include "sdg_stage.cuh"
+
+namespace sdg {
+int launch_stage_p8(int prec, int opt, const StageArgs& a, cudaStream_t st) {
+  return launch_stage_order<8>(prec, opt, a, st);
+}
+int launch_stage_p9(int prec, int opt, const StageArgs& a, cudaStream_t st) {
+  return launch_stage_order<9>(prec, opt, a, st);
+}
+}  // namespace sdg

@@ -1,0 +1,65 @@
+"""Shared helpers for the tests: building cases and comparing results."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+import oracle as O
+import workloads as W
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+# The reference's operator files; present only where the reference is mounted.
+REF_OPDATA = "/root/reference/operator_data"
+
+# tolerances stated by the parity contract
+TOL_TEND = 1e-12     # relative L2 per tendency (plain FP64 form)
+TOL_RUN = 1e-10      # relative L2 of q after nstep (plain FP64 form)
+TOL_FP32 = 1e-5      # relative L2 of the FP32-compute form against FP64
+
+
+def rel_l2(x, ref) -> float:
+    x = np.asarray(x, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    den = np.linalg.norm(ref)
+    return float(np.linalg.norm(x - ref) / (den if den > 0 else 1.0))
+
+
+def operators(p: int):
+    """(x1D, D1D, D1D_tr, Lift) from the product's generator."""
+    import sdg
+    return sdg.operator_generate(p)
+
+
+class Case:
+    """A periodic box with fields, built by the oracle like main.f90's init."""
+
+    def __init__(self, NeX, NeY, NeZ, p, ic="blob", seed=W.BASE_SEED, vel=(1.0, 0.5, 0.25),
+                 ops=None):
+        self.NeX, self.NeY, self.NeZ, self.p = NeX, NeY, NeZ, p
+        self.x1D, self.D, self.Dt, self.Lift = ops if ops is not None else operators(p)
+        self.mesh = O.Mesh(NeX, NeY, NeZ, p, self.x1D)
+        m = self.mesh
+        if ic == "sine":
+            q, u, v, w = W.sine(NeX, NeY, NeZ, self.x1D, vel)
+        else:
+            q, u, v, w = W.blob(NeX, NeY, NeZ, self.x1D, seed)
+        self.q, self.u, self.v, self.w = (W.with_halo(a, m.NeA, m.Np) for a in (q, u, v, w))
+        for f in (self.q, self.u, self.v, self.w):
+            m.update_halo(f)
+        self.dt = W.cfl_dt(NeX, NeY, NeZ, p, u, v, w)
+
+    @property
+    def nown(self) -> int:
+        return self.mesh.Np * self.mesh.Ne
+
+    def oracle_tend(self, opt=O.OPT1):
+        return O.cal_tend(self.mesh, self.q, self.u, self.v, self.w, self.D, self.Dt, self.Lift,
+                          opt)[: self.nown]
+
+    def oracle_run(self, nstep, opt=O.OPT1):
+        q = self.q.copy()
+        O.run(self.mesh, q, self.u, self.v, self.w, self.D, self.Dt, self.Lift, self.dt, nstep,
+              opt)
+        return q[: self.nown]

@@ -1,0 +1,238 @@
+"""GPU parity: every CUDA entry point against the CPU oracle on the same
+inputs, through the C ABI.  Tolerances: relative L2 <= 1e-12 per tendency and
+<= 1e-10 after nstep for the FP64 form; <= 1e-5 for the FP32-compute form."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import sdg
+import workloads as W
+from helpers import GOLDEN, TOL_FP32, TOL_RUN, TOL_TEND, Case, operators, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def mesh_dims(p):
+    if p <= 3:
+        return (4, 3, 5)
+    if p <= 7:
+        return (3, 2, 4)
+    return (2, 2, 3)
+
+
+def solver_for(c: Case, opt=sdg.OPT_OPT1, prec=sdg.PREC_FP64):
+    s = sdg.Solver(c.NeX, c.NeY, c.NeZ, c.p, c.D, c.Lift, opt=opt, precision=prec)
+    n = c.nown
+    s.upload(c.q[:n], c.u[:n], c.v[:n], c.w[:n])
+    return s
+
+
+@pytest.mark.parametrize("p", range(1, 16))
+@pytest.mark.parametrize("opt", [sdg.OPT_OPT1, sdg.OPT_GENERAL])
+def test_fused_stage_tendency_matches_oracle(p, opt):
+    c = Case(*mesh_dims(p), p, ic="blob")
+    s = solver_for(c, opt)
+    dq = s.tendency()
+    ref = c.oracle_tend(opt)
+    assert rel_l2(dq, ref) <= TOL_TEND
+
+
+@pytest.mark.parametrize("p,dims,nstep,ic", [
+    (3, (8, 8, 8), 100, "sine"),      # the reference-sized CPU case
+    (7, (4, 3, 2), 20, "blob"),
+    (10, (2, 2, 2), 5, "blob"),
+    (1, (1, 2, 3), 30, "blob"),       # elements that are their own x-neighbour
+])
+def test_solver_run_matches_oracle(p, dims, nstep, ic):
+    c = Case(*dims, p, ic=ic)
+    s = solver_for(c)
+    s.step(c.dt, nstep)
+    q = s.download()
+    assert rel_l2(q, c.oracle_run(nstep)) <= TOL_RUN
+
+
+def test_solver_steps_compose():
+    c = Case(3, 3, 2, 4, ic="blob")
+    a = solver_for(c)
+    a.step(c.dt, 6)
+    b = solver_for(c)
+    for _ in range(3):
+        b.step(c.dt, 2)
+    assert np.array_equal(a.download(), b.download())
+
+
+@pytest.mark.parametrize("p", [1, 3, 7, 8, 12])
+@pytest.mark.parametrize("opt", ["OPT1", "GENERAL"])
+def test_dropin_cal_tend_matches_oracle(p, opt):
+    c = Case(*mesh_dims(p), p, ic="blob")
+    m = c.mesh
+    sdg.dg_optr_kernel_setup(opt)
+    dqdt = np.full(m.Np * m.NeA, 7.0)
+    sdg.advect3d_eq_cal_tend(dqdt, c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, m.VMapM, m.VMapP,
+                             m.normal_fn, m.Escale, m.Fscale, m.Nq, m.Np, m.NfpTot, m.Ne, m.NeA)
+    ref = c.oracle_tend(O.OPT1 if opt == "OPT1" else O.GENERAL)
+    assert rel_l2(dqdt[: c.nown], ref) <= TOL_TEND
+    assert np.all(dqdt[c.nown:] == 7.0)  # only dqdt(:,1:Ne) is written
+
+
+def test_dropin_rejects_out_of_range_vmap():
+    c = Case(2, 2, 2, 2, ic="blob")
+    m = c.mesh
+    sdg.dg_optr_kernel_setup("OPT1")
+    bad = m.VMapP.copy()
+    bad[17] = m.Np * m.NeA + 1
+    with pytest.raises(sdg.SdgError) as e:
+        sdg.advect3d_eq_cal_tend(np.zeros(m.Np * m.NeA), c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift,
+                                 m.VMapM, bad, m.normal_fn, m.Escale, m.Fscale, m.Nq, m.Np,
+                                 m.NfpTot, m.Ne, m.NeA)
+    assert e.value.status == sdg.ERR_MESH
+
+
+@pytest.mark.parametrize("p", [1, 5, 9, 15])
+def test_operator_kernels_match_oracle(p):
+    sdg.dg_optr_kernel_setup("OPT1")
+    x, D, Dt, L = operators(p)
+    Nq, Np = p + 1, (p + 1) ** 3
+    rng = np.random.default_rng(p)
+    nel = 5
+    fx, fy, fz = (rng.standard_normal(Np * nel) for _ in range(3))
+    ox, oy, oz = sdg.tensorprod_divlike_dirXYZ(D, Dt, fx, fy, fz, Nq)
+    fl = rng.standard_normal(6 * Nq * Nq * nel)
+    lo = sdg.tensorprod_Lift_hexahedral(L, fl, Nq)
+    for e in range(nel):
+        s = slice(e * Np, (e + 1) * Np)
+        rx, ry, rz = O.divlike(D, Dt, fx[s], fy[s], fz[s], Nq, O.OPT1)
+        for got, ref in ((ox[s], rx), (oy[s], ry), (oz[s], rz)):
+            assert np.max(np.abs(got - ref)) <= 1e-14 * np.abs(D).max() * np.abs(fx).max() * Nq
+        rl = O.lift(L, fl[e * 6 * Nq * Nq:(e + 1) * 6 * Nq * Nq], Nq)
+        assert np.max(np.abs(lo[s] - rl)) <= 1e-14 * np.abs(L).max() * 6 * np.abs(fl).max()
+
+
+def test_dev_update_halo_and_rk_stage_match_oracle():
+    c = Case(3, 2, 2, 3, ic="blob")
+    m = c.mesh
+    q = c.q.copy()
+    q[m.Np * m.Ne:] = 0.0
+    dq = sdg.DeviceArray(q)
+    hm = sdg.DeviceArray(m.halo_src_map)
+    assert sdg.lib.sdg_update_halo_dev(dq.ptr, hm.ptr, m.Np, m.Ne, m.NhaloNode, None) == 0
+    ref = q.copy()
+    m.update_halo(ref)
+    assert np.array_equal(dq.numpy(), ref)
+    rng = np.random.default_rng(3)
+    q0 = rng.standard_normal(c.nown)
+    t = rng.standard_normal(c.nown)
+    for stage in (1, 2, 3):
+        qq = rng.standard_normal(c.nown)
+        dqq, dq0, dt_ = sdg.DeviceArray(qq), sdg.DeviceArray(q0), sdg.DeviceArray(t)
+        assert sdg.lib.sdg_rk_stage_dev(dqq.ptr, dq0.ptr, dt_.ptr, m.Np, m.Ne, stage, 0.01,
+                                        None) == 0
+        ref = qq.copy()
+        O.rk_stage(ref, q0, t, m.Np, m.Ne, stage - 1, 0.01)
+        assert np.max(np.abs(dqq.numpy() - ref)) <= 4e-16 * np.abs(ref).max()
+
+
+def test_dev_cal_tend_sets_error_flag():
+    c = Case(2, 2, 1, 2, ic="blob")
+    m = c.mesh
+    bad = m.VMapM.copy()
+    bad[0] = 0
+    arrs = [sdg.DeviceArray(a) for a in (c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, bad, m.VMapP,
+                                         m.normal_fn, m.Escale, m.Fscale)]
+    out = sdg.DeviceArray(n=m.Np * m.NeA)
+    flux = sdg.DeviceArray(n=m.NfpTot * m.Ne)
+    err = sdg.DeviceArray(np.zeros(1, dtype=np.int32))
+    st = sdg.lib.sdg_advect3d_eq_cal_tend_dev(out.ptr, *[a.ptr for a in arrs], m.Nq, m.Np,
+                                              m.NfpTot, m.Ne, m.NeA, sdg.OPT_OPT1, flux.ptr,
+                                              err.ptr, None)
+    assert st == 0
+    sdg.synchronize()
+    assert err.numpy()[0] == 1
+
+
+def test_check_mesh_accepts_reference_mesh_and_rejects_others():
+    c = Case(3, 2, 2, 2, ic="blob")
+    m = c.mesh
+    s = solver_for(c)
+    s.check_mesh(m.VMapM, m.VMapP, m.normal_fn, m.Escale, m.Fscale)
+    bad = m.VMapP.copy()
+    bad[5], bad[6] = bad[6], bad[5]
+    with pytest.raises(sdg.SdgError) as e:
+        s.check_mesh(m.VMapM, bad, m.normal_fn, m.Escale, m.Fscale)
+    assert e.value.status == sdg.ERR_MESH
+
+
+@pytest.mark.parametrize("p", [2, 5, 7, 11])
+def test_fp32_compute_form_error_and_mass(p):
+    c = Case(*mesh_dims(p), p, ic="blob")
+    s = solver_for(c, prec=sdg.PREC_FP32)
+    nstep = 10
+    s.step(c.dt, nstep)
+    q = s.download()
+    ref = c.oracle_run(nstep)
+    assert rel_l2(q, ref) <= TOL_FP32
+    m0 = W.mass(c.q, c.x1D, c.NeX, c.NeY, c.NeZ)
+    assert abs(W.mass(q, c.x1D, c.NeX, c.NeY, c.NeZ) - m0) <= 1e-6 * abs(m0)
+
+
+GOLDEN_FILES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+@pytest.mark.parametrize("path", GOLDEN_FILES, ids=[os.path.basename(p) for p in GOLDEN_FILES])
+def test_gpu_matches_golden_fixture(path):
+    g = np.load(path)
+    NeX, NeY, NeZ, p, nstep = (int(v) for v in g["dims"])
+    s = sdg.Solver(NeX, NeY, NeZ, p, g["D"], g["Lift"], opt=sdg.OPT_OPT1)
+    s.upload(g["q"], g["u"], g["v"], g["w"])
+    assert rel_l2(s.tendency(), g["dqdt_opt1"]) <= TOL_TEND
+    s.step(float(g["dt"]), nstep)
+    assert rel_l2(s.download(), g["q_final"]) <= TOL_RUN
+    s2 = sdg.Solver(NeX, NeY, NeZ, p, g["D"], g["Lift"], opt=sdg.OPT_GENERAL)
+    s2.upload(g["q"], g["u"], g["v"], g["w"])
+    assert rel_l2(s2.tendency(), g["dqdt_general"]) <= TOL_TEND
+
+
+# ---- full-size properties (p=7, 32^3: 16.8M DOF) -------------------------------
+
+@pytest.fixture(scope="module")
+def full_case():
+    p, N = 7, 32
+    x, D, Dt, L = operators(p)
+    q, u, v, w = W.blob(N, N, N, x, W.BASE_SEED)
+    return dict(p=p, N=N, x=x, D=D, Dt=Dt, L=L, q=q, u=u, v=v, w=w,
+                dt=W.cfl_dt(N, N, N, p, u, v, w))
+
+
+def test_full_size_tendency_matches_oracle(full_case):
+    f = full_case
+    N, p = f["N"], f["p"]
+    s = sdg.Solver(N, N, N, p, f["D"], f["L"])
+    s.upload(f["q"], f["u"], f["v"], f["w"])
+    dq = s.tendency()
+    m = O.Mesh(N, N, N, p, f["x"])
+    arrs = [W.with_halo(a, m.NeA, m.Np) for a in (f["q"], f["u"], f["v"], f["w"])]
+    for a in arrs:
+        m.update_halo(a)
+    ref = O.cal_tend(m, *arrs, f["D"], f["Dt"], f["L"], O.OPT1)[: m.Np * m.Ne]
+    assert rel_l2(dq, ref) <= TOL_TEND
+
+
+def test_full_size_mass_conservation_and_shift_invariance(full_case):
+    f = full_case
+    N, p, Np = f["N"], f["p"], (f["p"] + 1) ** 3
+    s = sdg.Solver(N, N, N, p, f["D"], f["L"])
+    s.upload(f["q"], f["u"], f["v"], f["w"])
+    m0 = W.mass(f["q"], f["x"], N, N, N)
+    s.step(f["dt"], 5)
+    q = s.download()
+    assert abs(W.mass(q, f["x"], N, N, N) - m0) <= 1e-12 * abs(m0)
+    # shifting every input by one element along x shifts the result exactly
+    def shift(a):
+        return np.roll(a.reshape(N, N, N, Np), 1, axis=2).reshape(-1)
+    s2 = sdg.Solver(N, N, N, p, f["D"], f["L"])
+    s2.upload(shift(f["q"]), shift(f["u"]), shift(f["v"]), shift(f["w"]))
+    s2.step(f["dt"], 5)
+    assert np.array_equal(s2.download(), shift(q))
