@@ -68,7 +68,7 @@ def _load() -> C.CDLL:
         "sdg_dg_optr_kernel_type": ([], _i),
         "sdg_advect3d_eq_cal_tend": ([_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip,
                                       _dp, _dp, _dp, _i, _i, _i, _i, _i], _i),
-        "sdg_advect3d_eq_cal_tend_dev": ([_vp] * 16 + [_i] * 6 + [_vp, _vp, _vp], _i),
+        "sdg_advect3d_eq_cal_tend_dev": ([_vp] * 13 + [_i] * 6 + [_vp, _vp, _vp], _i),
         "sdg_tensorprod_divlike_dirXYZ": ([_dp] * 8 + [_i, _i], _i),
         "sdg_tensorprod_divlike_dirXYZ_dev": ([_vp] * 8 + [_i, _i, _i, _vp], _i),
         "sdg_tensorprod_Lift_hexahedral": ([_dp, _dp, _dp, _i, _i], _i),
