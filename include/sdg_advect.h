@@ -123,6 +123,32 @@ int sdg_advect3d_eq_cal_tend_dev(double* dqdt, const double* q,
                                  int opt, double* flux_scratch, int* err_flag,
                                  void* stream);
 
+/* Allocation-free form of sdg_advect3d_eq_cal_tend_dev; it has no
+ * counterpart in the reference.  For callers that cannot allocate device
+ * memory when they need the tendency: a host model that pre-reserves its HBM
+ * through its own pool, a request loop that cannot afford the device-wide
+ * synchronisation of cudaFree, or code that must not fail for lack of memory
+ * mid-step.  The flux scratch and the error flag live in a fixed device array
+ * inside the library (16 MiB, held by every GPU that loads the library until
+ * exit), so a call allocates nothing; a call needing more than 2^21
+ * face-flux values (NfpTot*Ne) is rejected with SDG_ERR_INVALID_ARG.  All
+ * calls on a device share that array: calls whose work overlaps on the GPU
+ * race and must be serialised by the caller.  The first call on a device
+ * looks up the array's device address, so make it before any stream
+ * capture.  Synchronous: waits for `stream` and returns SDG_ERR_MESH when a
+ * VMap entry is out of range. */
+int sdg_advect3d_eq_cal_tend_noalloc(double* dqdt, const double* q,
+                                     const double* u, const double* v,
+                                     const double* w, const double* D1D,
+                                     const double* D1D_tr,
+                                     const double* Lift_mat, const int* VMapM,
+                                     const int* VMapP,
+                                     const double* normal_fn,
+                                     const double* Escale,
+                                     const double* Fscale, int Nq, int Np,
+                                     int NfpTot, int Ne, int NeA, int opt,
+                                     void* stream);
+
 /* tensorprod_divlike_dirXYZ (mod_dg_optr_kernel.f90:62-136) over nelem
  * consecutive elements (nelem = 1 is the reference call made per element from
  * mod_advect3d_eq.f90:185-188).  Each array holds nelem blocks of Nq^3
