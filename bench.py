@@ -36,7 +36,8 @@ sys.path.insert(0, PKG)
 
 # algorithmic bytes per DOF-update: stage 1 reads q,u,v,w and writes q (40 B);
 # stages 2 and 3 also read q0 (48 B).  FP32 form: velocity in FP32.
-BYTES_PER_DOF_UPDATE = {"fp64": 136.0 / 3.0, "fp32": 100.0 / 3.0}
+BYTES_PER_DOF_UPDATE = {"fp64": 136.0 / 3.0, "fp64emu": 136.0 / 3.0, "fp32": 100.0 / 3.0}
+PRECISIONS = {"fp64": 0, "fp32": 1, "fp64emu": 2}
 
 
 def flops_per_dof_update(p: int) -> float:
@@ -130,25 +131,41 @@ def make_workload(p: int, ne: int, seed: int):
     return dict(x=x, D=D, Dt=Dt, L=L, q=q, u=u, v=v, w=w, dt=dt)
 
 
-def time_oracle(wl, p, ne, min_seconds: float, max_steps: int, warmup: int = 0):
-    """Runs the oracle (C + OpenMP) step by step; returns (steps, seconds, threads)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    import workloads as W
-    m = O.Mesh(ne, ne, ne, p, wl["x"])
-    arrs = [W.with_halo(a, m.NeA, m.Np) for a in (wl["q"], wl["u"], wl["v"], wl["w"])]
-    for a in arrs:
-        m.update_halo(a)
-    q = arrs[0]
-    for _ in range(warmup):
-        O.run(m, q, arrs[1], arrs[2], arrs[3], wl["D"], wl["Dt"], wl["L"], wl["dt"], 1, O.OPT1)
-    steps, t0 = 0, time.perf_counter()
-    while steps < max_steps:
-        O.run(m, q, arrs[1], arrs[2], arrs[3], wl["D"], wl["Dt"], wl["L"], wl["dt"], 1, O.OPT1)
-        steps += 1
-        if time.perf_counter() - t0 >= min_seconds:
-            break
-    return steps, time.perf_counter() - t0, O.num_threads()
+class OracleBox:
+    """The CPU oracle (C + OpenMP) set up on the bench workload: mesh arrays,
+    fields with halos, the tendency of the initial state, and timed steps."""
+
+    def __init__(self, wl, p, ne):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        import workloads as W
+        self.O, self.wl = O, wl
+        self.m = O.Mesh(ne, ne, ne, p, wl["x"])
+        self.arrs = [W.with_halo(a, self.m.NeA, self.m.Np)
+                     for a in (wl["q"], wl["u"], wl["v"], wl["w"])]
+        for a in self.arrs:
+            self.m.update_halo(a)
+        self.threads = O.num_threads()
+
+    def tendency(self):
+        m = self.m
+        return self.O.cal_tend(m, *self.arrs, self.wl["D"], self.wl["Dt"], self.wl["L"],
+                               self.O.OPT1)[: m.Np * m.Ne]
+
+    def time_steps(self, min_seconds: float, max_steps: int, warmup: int = 0):
+        """Steps a copy of the state; returns (steps, seconds)."""
+        O, wl, m = self.O, self.wl, self.m
+        q = self.arrs[0].copy()
+        args = (self.arrs[1], self.arrs[2], self.arrs[3], wl["D"], wl["Dt"], wl["L"], wl["dt"])
+        for _ in range(warmup):
+            O.run(m, q, *args[:3], *args[3:6], args[6], 1, O.OPT1)
+        steps, t0 = 0, time.perf_counter()
+        while steps < max_steps:
+            O.run(m, q, *args[:3], *args[3:6], args[6], 1, O.OPT1)
+            steps += 1
+            if time.perf_counter() - t0 >= min_seconds:
+                break
+        return steps, time.perf_counter() - t0
 
 
 def load_traffic(key: str):
@@ -167,7 +184,9 @@ def run_reference(args, ws, rank):
     wl = make_workload(args.p, args.ne, args.seed)
     ndof = (args.p + 1) ** 3 * args.ne ** 3
     # warm-up steps, then K timed steps of the same workload
-    steps, secs, threads = time_oracle(wl, args.p, args.ne, 0.0, args.steps, args.warmup)
+    ob = OracleBox(wl, args.p, args.ne)
+    steps, secs = ob.time_steps(0.0, args.steps, args.warmup)
+    threads = ob.threads
     v = ndof * 3 * steps / secs / 1e9
     line = {
         "impl": "reference",
@@ -187,13 +206,17 @@ def run_reference(args, ws, rank):
     return 0
 
 
+PREC_LABEL = {"fp64": "FP64", "fp64emu": "FP64 state, double-float arithmetic",
+              "fp32": "FP32-compute/FP64-state"}
+
+
 def metric_name(args) -> str:
-    return f"GDOF-updates/s (p={args.p}, {args.ne}^3, {'FP64' if args.precision == 'fp64' else 'FP32-compute/FP64-state'})"
+    return f"GDOF-updates/s (p={args.p}, {args.ne}^3, {PREC_LABEL[args.precision]})"
 
 
 def config(args) -> dict:
     ndof = (args.p + 1) ** 3 * args.ne ** 3
-    ws_bytes = ndof * (8 * 3 + (24 if args.precision == "fp64" else 12))
+    ws_bytes = ndof * (8 * 3 + (12 if args.precision == "fp32" else 24))
     return {"workload": f"3D DG advection, periodic unit box, Ne={args.ne}^3, p={args.p}, "
                         f"SSP-RK3, CFL 0.1, {args.precision} plain form",
             "p": args.p, "Ne": [args.ne] * 3, "dof": ndof, "opt": "OPT1",
@@ -201,6 +224,56 @@ def config(args) -> dict:
             "l2": f"inputs larger than L2 (state+velocity working set {ws_bytes / 1e6:.0f} MB "
                   "vs 129 MB L2)",
             "parallelism": "replicas (one independent box per GPU)"}
+
+
+def time_solver(sdg, wl, p, ne, prec, steps, warmup, local, barrier, sample_clocks):
+    """Uploads the workload, warms up, and times `steps` steps with CUDA events
+    on the solver's stream.  Returns (solver, seconds, clocks)."""
+    s = sdg.Solver(ne, ne, ne, p, wl["D"], wl["L"], opt=sdg.OPT_OPT1, precision=prec)
+    s.upload(wl["q"], wl["u"], wl["v"], wl["w"])
+    s.step(wl["dt"], warmup)
+    sdg.synchronize()
+    clocks = ClockSampler(local) if sample_clocks else None
+    barrier()
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)  # let the sampler start
+    ms = s.step_timed(wl["dt"], steps)
+    sdg.synchronize()
+    clk = clocks.stop() if clocks else None
+    barrier()
+    return s, ms / 1e3, clk
+
+
+def roofline(precision, p, ne, ndof, t, steps, peaks):
+    launches = 3 * steps
+    avg_launch = t / launches
+    bpd = BYTES_PER_DOF_UPDATE[precision]
+    achieved = bpd * ndof / avg_launch / 1e9
+    peak, peak_kind = measured_peaks()
+    per_gpu = ndof * 3 * steps / t / 1e9
+    fl = flops_per_dof_update(p)
+    pipe = "dfma_tflops" if precision == "fp64" else "ffma_tflops"
+    kernel = {"fp64": f"stage_kernel<{p},double>", "fp32": f"stage_kernel<{p},float>",
+              "fp64emu": f"stage_emu_kernel<{p}>"}[precision]
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak,
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "algorithmic_bytes_per_dof_update": bpd,
+            "traffic": load_traffic(f"stage_{precision}_p{p}_ne{ne}"),
+            "kernel": kernel, "avg_launch_ms": avg_launch * 1e3}
+    if peaks is not None:
+        roof["compute"] = {
+            "pipe": "FP64 (DFMA)" if precision == "fp64" else "FP32 (FFMA)",
+            "flops_per_dof_update": fl,
+            "achieved_tflops": fl * per_gpu / 1e3,
+            "peak_tflops_measured_live": peaks[pipe],
+            "frac": fl * per_gpu / 1e3 / peaks[pipe],
+            "note": ("algorithmic FP64 flops; the emulated path spends ~20 FP32 ops per "
+                     "FP64 flop" if precision == "fp64emu" else "algorithmic flops")}
+        if precision == "fp64":
+            roof["binding_roof"] = "fp64_pipe" if roof["compute"]["frac"] > roof["frac"] else "hbm"
+    return roof
 
 
 def run_ours(args, ws, rank, local):
@@ -217,55 +290,25 @@ def run_ours(args, ws, rank, local):
         if dist is not None:
             dist.barrier()
 
-    p, ne = args.p, args.ne
-    prec = sdg.PREC_FP64 if args.precision == "fp64" else sdg.PREC_FP32
-    wl = make_workload(p, ne, args.seed + rank)
-    ndof = (p + 1) ** 3 * ne ** 3
-    s = sdg.Solver(ne, ne, ne, p, wl["D"], wl["L"], opt=sdg.OPT_OPT1, precision=prec)
-    s.upload(wl["q"], wl["u"], wl["v"], wl["w"])
-    s.step(wl["dt"], args.warmup)
-    sdg.synchronize()
-
-    # ---- device-resident timing (CUDA events on the solver's stream) ----
-    clocks = ClockSampler(local)
-    barrier()
-    sdg.synchronize()
-    clocks.start()
-    time.sleep(0.3)  # let the sampler start
-    t_wall0 = time.perf_counter()
-    ms = s.step_timed(wl["dt"], args.steps)
-    sdg.synchronize()
-    t_wall = time.perf_counter() - t_wall0
-    clk = clocks.stop()
-    barrier()
-    t = ms / 1e3
-    if dist is not None:
+    def tmax(t):
+        if dist is None:
+            return t
         import torch
         tt = torch.tensor([t], dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
-    value = ws * ndof * 3 * args.steps / t / 1e9
-    per_gpu = ndof * 3 * args.steps / t / 1e9
+        return float(tt.item())
 
-    # ---- roofline of the fused stage kernel (the only kernel in a step) ----
-    launches = 3 * args.steps
-    avg_launch = t / launches
-    bpd = BYTES_PER_DOF_UPDATE[args.precision]
-    achieved = bpd * ndof / avg_launch / 1e9
-    peak, peak_kind = measured_peaks()
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-            "algorithmic_bytes_per_dof_update": bpd,
-            "traffic": load_traffic(f"stage_{args.precision}_p{p}_ne{ne}"),
-            "kernel": f"stage_kernel<{p},{'double' if prec == 0 else 'float'}>",
-            "avg_launch_ms": avg_launch * 1e3}
-    fl = flops_per_dof_update(p)
-    pk = sdg.microbench_peaks()
-    pipe = "dfma_tflops" if args.precision == "fp64" else "ffma_tflops"
-    roof["compute"] = {"pipe": "FP64 (DFMA)" if args.precision == "fp64" else "FP32 (FFMA)",
-                       "flops_per_dof_update": fl, "achieved_tflops": fl * per_gpu / 1e3,
-                       "peak_tflops_measured_live": pk[pipe],
-                       "frac": fl * per_gpu / 1e3 / pk[pipe]}
+    p, ne = args.p, args.ne
+    wl = make_workload(p, ne, args.seed + rank)
+    ndof = (p + 1) ** 3 * ne ** 3
+
+    # ---- headline: the requested precision, device-resident ----
+    s, t, clk = time_solver(sdg, wl, p, ne, PRECISIONS[args.precision], args.steps,
+                            args.warmup, local, barrier, True)
+    t = tmax(t)
+    value = ws * ndof * 3 * args.steps / t / 1e9
+    peaks = None if args.no_microbench else sdg.microbench_peaks()
+    roof = roofline(args.precision, p, ne, ndof, t, args.steps, peaks)
 
     # ---- end to end through the C ABI with pinned host buffers ----
     e2e = None
@@ -274,8 +317,7 @@ def run_ours(args, ws, rank, local):
         for pa, src in zip(pins, (wl["q"], wl["u"], wl["v"], wl["w"])):
             pa.array[:] = src
         k = max(1, min(args.steps, args.e2e_steps))
-        # one untimed round trip
-        s.upload_ptrs(*(pa.ptr for pa in pins[:4]))
+        s.upload_ptrs(*(pa.ptr for pa in pins[:4]))  # one untimed round trip
         s.step(wl["dt"], 1)
         s.download_ptr(pins[4].ptr)
         barrier()
@@ -284,18 +326,35 @@ def run_ours(args, ws, rank, local):
             s.upload_ptrs(*(pa.ptr for pa in pins[:4]))
             s.step(wl["dt"], 1)
             s.download_ptr(pins[4].ptr)  # synchronises the stream
-        te = time.perf_counter() - t0
-        if dist is not None:
-            import torch
-            tt = torch.tensor([te], dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            te = float(tt.item())
+        te = tmax(time.perf_counter() - t0)
         e2e = {"value": ws * ndof * 3 * k / te / 1e9, "unit": "GDOF-updates/s",
                "h2d_bytes_per_step": 4 * 8 * ndof, "d2h_bytes_per_step": 8 * ndof,
                "steps": k, "path": "sdg_solver_upload + sdg_solver_step + sdg_solver_download"}
         for pa in pins:
             pa.free()
+    tend_main = None
+    if rank == 0 and not args.no_cpu_baseline:
+        s.upload(wl["q"], wl["u"], wl["v"], wl["w"])  # the initial state again
+        tend_main = s.tendency()
     s.close()
+
+    # ---- the other FP64-state path on the same workload ----
+    other = None
+    if args.precision == "fp64" and not args.no_emu:
+        se, te_, _ = time_solver(sdg, wl, p, ne, PRECISIONS["fp64emu"], args.steps,
+                                 args.warmup, local, barrier, False)
+        te_ = tmax(te_)
+        other = {"precision": "fp64emu",
+                 "description": "FP64 state and RK combine; flux, divergence and lift in "
+                                "double-float (two FP32 numbers) on the FP32 pipes",
+                 "value": ws * ndof * 3 * args.steps / te_ / 1e9, "unit": "GDOF-updates/s",
+                 "ms_per_step": 1e3 * te_ / args.steps,
+                 "roofline": roofline("fp64emu", p, ne, ndof, te_, args.steps, peaks)}
+        tend_emu = None
+        if rank == 0 and not args.no_cpu_baseline:
+            se.upload(wl["q"], wl["u"], wl["v"], wl["w"])
+            tend_emu = se.tendency()
+        se.close()
 
     if rank != 0:
         if dist is not None:
@@ -303,21 +362,39 @@ def run_ours(args, ws, rank, local):
         return 0
 
     cpu = None
-    if ws == 1 and not args.no_cpu_baseline:
-        steps, secs, threads = time_oracle(wl, p, ne, args.cpu_seconds, 10 ** 6)
-        cpu = {"value": ndof * 3 * steps / secs / 1e9, "unit": "GDOF-updates/s", "cores": threads,
-               "kind": "port",
-               "sample": f"{steps} SSP-RK3 steps of the same {ne}^3 p={p} box in FP64 "
-                         f"({secs:.1f} s; C + OpenMP restatement of the Fortran reference)"}
+    parity = None
+    if not args.no_cpu_baseline:
+        ob = OracleBox(wl, p, ne)
+        ref = ob.tendency()
+
+        def rl2(x):
+            return float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
+
+        parity = {"tendency_rel_l2_vs_oracle": {args.precision: rl2(tend_main)},
+                  "tolerance": 1e-12 if args.precision != "fp32" else 1e-5,
+                  "state": "initial state of the bench workload"}
+        if other is not None:
+            parity["tendency_rel_l2_vs_oracle"]["fp64emu"] = rl2(tend_emu)
+            other["tendency_rel_l2_vs_fp64_oracle"] = rl2(tend_emu)
+        if ws == 1:
+            steps, secs = ob.time_steps(args.cpu_seconds, 10 ** 6)
+            cpu = {"value": ndof * 3 * steps / secs / 1e9, "unit": "GDOF-updates/s",
+                   "cores": ob.threads, "kind": "port",
+                   "sample": f"{steps} SSP-RK3 steps of the same {ne}^3 p={p} box in FP64 "
+                             f"({secs:.1f} s; C + OpenMP restatement of the Fortran "
+                             "reference)"}
     line = {
         "metric": metric_name(args), "value": value, "unit": "GDOF-updates/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32-compute/f64-state",
+        "dtype": {"fp64": "f64", "fp64emu": "f64-state/double-float",
+                  "fp32": "f32-compute/f64-state"}[args.precision],
         "data": "synthetic (seeded Gaussian tracer, seeded smooth velocity)",
         "config": config(args), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": launches, "clocks": clk, "wall_s_timed_region": t_wall,
+        "gpu_launches": 3 * args.steps, "clocks": clk, "parity": parity,
     }
+    if other is not None:
+        line["fp64_emulated"] = other
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -327,17 +404,21 @@ def run_ours(args, ws, rank, local):
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--p", type=int, default=7)
     ap.add_argument("--ne", type=int, default=32)
-    ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "fp64emu", "fp32"], default="fp64")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-emu", action="store_true",
+                    help="skip the emulated-FP64 measurement beside the FP64 headline")
+    ap.add_argument("--no-microbench", action="store_true",
+                    help="skip the live DFMA/FFMA peak measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -59,6 +59,7 @@ struct StageArgs {
   long long elem_begin;  // first element of this launch
   long long elem_count;  // elements of this launch
   double a, b, dt;      // q_out = a*q0 + b*(q_in + dt*dqdt)
+  float cdt_hi, cdt_lo; // b*dt as a double-float pair (emulated-FP64 kernel)
   int tend_only;        // write dqdt instead of the RK update
 };
 

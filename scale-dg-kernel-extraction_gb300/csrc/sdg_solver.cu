@@ -5,9 +5,11 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstring>
 #include <new>
 #include <vector>
 
+#include "sdg_df.cuh"
 #include "sdg_internal.h"
 
 using namespace sdg;
@@ -33,6 +35,14 @@ __global__ void f64_to_f32_kernel(float* out, const double* in, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     out[i] = (float)in[i];
+}
+
+__global__ void f64_to_df_kernel(float2* out, const double* in, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const dfl d = df_from_double(in[i]);
+    out[i] = make_float2(d.hi, d.lo);
+  }
 }
 
 unsigned grid_for(long long n) {
@@ -70,6 +80,9 @@ int one_stage(sdg_solver* s, int stage, double dt, const double* qin,
   a.a = rk_a[stage];
   a.b = rk_b[stage];
   a.dt = dt;
+  const dfl cdt = df_from_double(a.b * dt);
+  a.cdt_hi = cdt.hi;
+  a.cdt_lo = cdt.lo;
   a.tend_only = tend_only ? 1 : 0;
   return launch_stage(s->p, s->prec, s->opt, a, s->stream);
 }
@@ -80,12 +93,58 @@ int put_velocity(sdg_solver* s, void* dst, const double* src_dev) {
   if (s->prec == SDG_PREC_FP64) {
     SDG_CUDA_TRY(cudaMemcpyAsync(dst, src_dev, 8 * (size_t)n, cudaMemcpyDeviceToDevice,
                                  s->stream));
+  } else if (s->prec == SDG_PREC_FP64_EMU) {
+    f64_to_df_kernel<<<grid_for(n), 256, 0, s->stream>>>(static_cast<float2*>(dst), src_dev, n);
+    SDG_CUDA_TRY(cudaGetLastError());
   } else {
     f64_to_f32_kernel<<<grid_for(n), 256, 0, s->stream>>>(static_cast<float*>(dst),
                                                          src_dev, n);
     SDG_CUDA_TRY(cudaGetLastError());
   }
   return SDG_OK;
+}
+
+// Operator tables in the layout and arithmetic each kernel family reads:
+//   FP64: D1D(Nq,Nq) and Lift_mat(Nq,Nq,Nq,6) as given;
+//   FP32: the same rounded to float;
+//   FP64_EMU: double-float tables with the geometric factors folded in:
+//     D: [6][Nq*Nq] floats = hi/lo planes of Es_x*D1D, Es_y*D1D, Es_z*D1D;
+//     Lift: [2][6*Np] floats = hi then lo plane of Lift_mat(n,f)*0.5*Fscale(f).
+void operator_tables(int prec, int Nq, const Box& box, const double* D1D,
+                     const double* Lift_mat, std::vector<unsigned char>& dtab,
+                     std::vector<unsigned char>& ltab) {
+  const size_t nD = (size_t)Nq * Nq, Np = (size_t)Nq * Nq * Nq, nL = 6 * Np;
+  if (prec == SDG_PREC_FP64) {
+    dtab.resize(8 * nD);
+    ltab.resize(8 * nL);
+    std::memcpy(dtab.data(), D1D, 8 * nD);
+    std::memcpy(ltab.data(), Lift_mat, 8 * nL);
+  } else if (prec == SDG_PREC_FP32) {
+    dtab.resize(4 * nD);
+    ltab.resize(4 * nL);
+    float* d = reinterpret_cast<float*>(dtab.data());
+    float* l = reinterpret_cast<float*>(ltab.data());
+    for (size_t i = 0; i < nD; i++) d[i] = (float)D1D[i];
+    for (size_t i = 0; i < nL; i++) l[i] = (float)Lift_mat[i];
+  } else {
+    dtab.resize(4 * 6 * nD);
+    ltab.resize(4 * 2 * nL);
+    float* d = reinterpret_cast<float*>(dtab.data());
+    float* l = reinterpret_cast<float*>(ltab.data());
+    for (int ax = 0; ax < 3; ax++)
+      for (size_t i = 0; i < nD; i++) {
+        const dfl v = df_from_double(box.Es[ax] * D1D[i]);
+        d[(2 * ax) * nD + i] = v.hi;
+        d[(2 * ax + 1) * nD + i] = v.lo;
+      }
+    const int face_axis[6] = {1, 0, 1, 0, 2, 2};  // -y,+x,+y,-x,-z,+z
+    for (int f = 0; f < 6; f++)
+      for (size_t n = 0; n < Np; n++) {
+        const dfl v = df_from_double(Lift_mat[n + f * Np] * (0.5 * box.Fs[face_axis[f]]));
+        l[n + f * Np] = v.hi;
+        l[nL + n + f * Np] = v.lo;
+      }
+  }
 }
 
 }  // namespace
@@ -107,7 +166,8 @@ int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
     return fail(SDG_ERR_INVALID_ARG, "too many elements");
   if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1)
     return fail(SDG_ERR_BAD_OPTTYPE, "unknown DGOptrKernel type %d", opt);
-  if (precision != SDG_PREC_FP64 && precision != SDG_PREC_FP32)
+  if (precision != SDG_PREC_FP64 && precision != SDG_PREC_FP32 &&
+      precision != SDG_PREC_FP64_EMU)
     return fail(SDG_ERR_INVALID_ARG, "unknown precision %d", precision);
   if (!D1D || !Lift_mat) return fail(SDG_ERR_INVALID_ARG, "NULL operator");
   SDG_TRY(require_device());
@@ -121,28 +181,25 @@ int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
   s->box = make_box(NeX, NeY, NeZ, Lx, Ly, Lz);
   s->ndof = (long long)s->Np * s->box.Ne;
   s->stream = as_stream(stream);
-  const size_t es = (precision == SDG_PREC_FP64) ? 8 : 4;
+  // velocity element size: FP64, FP32, or a double-float pair
+  const size_t es = (precision == SDG_PREC_FP32) ? 4 : 8;
   const size_t nD = (size_t)s->Nq * s->Nq, nL = 6 * (size_t)s->Np;
+  // operator tables as the kernels read them (see operator_tables below)
+  std::vector<unsigned char> dtab, ltab;
+  operator_tables(precision, s->Nq, s->box, D1D, Lift_mat, dtab, ltab);
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < 3 && e == cudaSuccess; i++)
     e = cudaMalloc(&s->q[i], 8 * (size_t)s->ndof);
   if (e == cudaSuccess) e = cudaMalloc(&s->u, es * (size_t)s->ndof);
   if (e == cudaSuccess) e = cudaMalloc(&s->v, es * (size_t)s->ndof);
   if (e == cudaSuccess) e = cudaMalloc(&s->w, es * (size_t)s->ndof);
-  if (e == cudaSuccess) e = cudaMalloc(&s->D, es * nD);
-  if (e == cudaSuccess) e = cudaMalloc(&s->Lift, es * nL);
-  if (e == cudaSuccess) {
-    if (precision == SDG_PREC_FP64) {
-      e = cudaMemcpy(s->D, D1D, 8 * nD, cudaMemcpyHostToDevice);
-      if (e == cudaSuccess) e = cudaMemcpy(s->Lift, Lift_mat, 8 * nL, cudaMemcpyHostToDevice);
-    } else {
-      std::vector<float> dF(nD), lF(nL);
-      for (size_t i = 0; i < nD; i++) dF[i] = (float)D1D[i];
-      for (size_t i = 0; i < nL; i++) lF[i] = (float)Lift_mat[i];
-      e = cudaMemcpy(s->D, dF.data(), 4 * nD, cudaMemcpyHostToDevice);
-      if (e == cudaSuccess) e = cudaMemcpy(s->Lift, lF.data(), 4 * nL, cudaMemcpyHostToDevice);
-    }
-  }
+  if (e == cudaSuccess) e = cudaMalloc(&s->D, dtab.size());
+  if (e == cudaSuccess) e = cudaMalloc(&s->Lift, ltab.size());
+  if (e == cudaSuccess) e = cudaMemcpy(s->D, dtab.data(), dtab.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(s->Lift, ltab.data(), ltab.size(), cudaMemcpyHostToDevice);
+  (void)nD;
+  (void)nL;
   if (e != cudaSuccess) {
     const int st = cuda_fail(e, "solver allocation", __FILE__, __LINE__);
     release(s);
@@ -231,7 +288,7 @@ int sdg_solver_upload(sdg_solver* s, const double* q, const double* u,
   if (!s || !q || !u || !v || !w) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
   const size_t bytes = 8 * (size_t)s->ndof;
   SDG_CUDA_TRY(cudaMemcpyAsync(s->q[s->cur], q, bytes, cudaMemcpyHostToDevice, s->stream));
-  if (s->prec == SDG_PREC_FP64) {
+  if (s->prec == SDG_PREC_FP64) {  // FP64 velocity is copied as is
     SDG_CUDA_TRY(cudaMemcpyAsync(s->u, u, bytes, cudaMemcpyHostToDevice, s->stream));
     SDG_CUDA_TRY(cudaMemcpyAsync(s->v, v, bytes, cudaMemcpyHostToDevice, s->stream));
     SDG_CUDA_TRY(cudaMemcpyAsync(s->w, w, bytes, cudaMemcpyHostToDevice, s->stream));

@@ -253,17 +253,4 @@ int launch_stage_impl(const StageArgs& a, cudaStream_t st) {
   return SDG_OK;
 }
 
-// Launches order P with the precision/optimisation choice resolved.
-template <int P>
-int launch_stage_order(int prec, int opt, const StageArgs& a, cudaStream_t st) {
-  constexpr bool kCanSplit = (P > 7);
-  const bool split = kCanSplit && (opt == SDG_OPT_OPT1);
-  if (prec == SDG_PREC_FP64) {
-    if (split) return launch_stage_impl<P, double, double, kCanSplit>(a, st);
-    return launch_stage_impl<P, double, double, false>(a, st);
-  }
-  if (split) return launch_stage_impl<P, float, float, kCanSplit>(a, st);
-  return launch_stage_impl<P, float, float, false>(a, st);
-}
-
 }  // namespace sdg

@@ -1,0 +1,23 @@
+// Per-order launch entry: resolves precision and summation order to one
+// instantiation of the fused stage kernels.
+#pragma once
+
+#include "sdg_stage.cuh"
+#include "sdg_stage_emu.cuh"
+
+namespace sdg {
+
+template <int P>
+int launch_stage_order(int prec, int opt, const StageArgs& a, cudaStream_t st) {
+  constexpr bool kCanSplit = (P > 7);
+  const bool split = kCanSplit && (opt == SDG_OPT_OPT1);
+  if (prec == SDG_PREC_FP64_EMU) return launch_stage_emu_impl<P>(a, st);
+  if (prec == SDG_PREC_FP64) {
+    if (split) return launch_stage_impl<P, double, double, kCanSplit>(a, st);
+    return launch_stage_impl<P, double, double, false>(a, st);
+  }
+  if (split) return launch_stage_impl<P, float, float, kCanSplit>(a, st);
+  return launch_stage_impl<P, float, float, false>(a, st);
+}
+
+}  // namespace sdg

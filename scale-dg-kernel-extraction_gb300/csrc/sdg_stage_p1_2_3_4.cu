@@ -1,6 +1,6 @@
 // Instantiations of the fused stage kernel for orders 1 2 3 4 (one translation
 // unit per group so that the build compiles them in parallel).
-#include "sdg_stage.cuh"
+#include "sdg_stage_order.cuh"
 
 namespace sdg {
 int launch_stage_p1(int prec, int opt, const StageArgs& a, cudaStream_t st) {

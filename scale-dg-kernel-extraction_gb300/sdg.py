@@ -35,6 +35,7 @@ OPT_GENERAL = 1
 OPT_OPT1 = 2
 PREC_FP64 = 0
 PREC_FP32 = 1
+PREC_FP64_EMU = 2
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")

@@ -40,15 +40,25 @@ def test_fused_stage_tendency_matches_oracle(p, opt):
     assert rel_l2(dq, ref) <= TOL_TEND
 
 
+@pytest.mark.parametrize("p", range(1, 16))
+@pytest.mark.parametrize("ic", ["blob", "sine"])
+def test_emulated_fp64_tendency_matches_oracle(p, ic):
+    """Double-float arithmetic on the FP32 pipes meets the FP64 tolerance."""
+    c = Case(*mesh_dims(p), p, ic=ic)
+    s = solver_for(c, prec=sdg.PREC_FP64_EMU)
+    assert rel_l2(s.tendency(), c.oracle_tend()) <= TOL_TEND
+
+
 @pytest.mark.parametrize("p,dims,nstep,ic", [
     (3, (8, 8, 8), 100, "sine"),      # the reference-sized CPU case
     (7, (4, 3, 2), 20, "blob"),
     (10, (2, 2, 2), 5, "blob"),
     (1, (1, 2, 3), 30, "blob"),       # elements that are their own x-neighbour
 ])
-def test_solver_run_matches_oracle(p, dims, nstep, ic):
+@pytest.mark.parametrize("prec", [sdg.PREC_FP64, sdg.PREC_FP64_EMU])
+def test_solver_run_matches_oracle(p, dims, nstep, ic, prec):
     c = Case(*dims, p, ic=ic)
-    s = solver_for(c)
+    s = solver_for(c, prec=prec)
     s.step(c.dt, nstep)
     q = s.download()
     assert rel_l2(q, c.oracle_run(nstep)) <= TOL_RUN
@@ -206,10 +216,11 @@ def full_case():
                 dt=W.cfl_dt(N, N, N, p, u, v, w))
 
 
-def test_full_size_tendency_matches_oracle(full_case):
+@pytest.mark.parametrize("prec", [sdg.PREC_FP64, sdg.PREC_FP64_EMU])
+def test_full_size_tendency_matches_oracle(full_case, prec):
     f = full_case
     N, p = f["N"], f["p"]
-    s = sdg.Solver(N, N, N, p, f["D"], f["L"])
+    s = sdg.Solver(N, N, N, p, f["D"], f["L"], precision=prec)
     s.upload(f["q"], f["u"], f["v"], f["w"])
     dq = s.tendency()
     m = O.Mesh(N, N, N, p, f["x"])
@@ -220,10 +231,11 @@ def test_full_size_tendency_matches_oracle(full_case):
     assert rel_l2(dq, ref) <= TOL_TEND
 
 
-def test_full_size_mass_conservation_and_shift_invariance(full_case):
+@pytest.mark.parametrize("prec", [sdg.PREC_FP64, sdg.PREC_FP64_EMU])
+def test_full_size_mass_conservation_and_shift_invariance(full_case, prec):
     f = full_case
     N, p, Np = f["N"], f["p"], (f["p"] + 1) ** 3
-    s = sdg.Solver(N, N, N, p, f["D"], f["L"])
+    s = sdg.Solver(N, N, N, p, f["D"], f["L"], precision=prec)
     s.upload(f["q"], f["u"], f["v"], f["w"])
     m0 = W.mass(f["q"], f["x"], N, N, N)
     s.step(f["dt"], 5)
@@ -232,7 +244,7 @@ def test_full_size_mass_conservation_and_shift_invariance(full_case):
     # shifting every input by one element along x shifts the result exactly
     def shift(a):
         return np.roll(a.reshape(N, N, N, Np), 1, axis=2).reshape(-1)
-    s2 = sdg.Solver(N, N, N, p, f["D"], f["L"])
+    s2 = sdg.Solver(N, N, N, p, f["D"], f["L"], precision=prec)
     s2.upload(shift(f["q"]), shift(f["u"]), shift(f["v"]), shift(f["w"]))
     s2.step(f["dt"], 5)
     assert np.array_equal(s2.download(), shift(q))
