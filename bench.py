@@ -276,6 +276,158 @@ def roofline(precision, p, ne, ndof, t, steps, peaks):
     return roof
 
 
+def ensemble_workload(n, seed):
+    """The batched-ensemble config: n instances, Ne per axis uniform in 4..24
+    independently per axis, p in {3,5,7}, Gaussian width uniform in
+    [0.05, 0.2], constant velocity of magnitude uniform in [0, 1] in a uniform
+    random direction, dt at CFL 0.1; drawn with splitmix64."""
+    import math
+    import workloads as W
+    members = []
+    for i in range(n):
+        r = W.SplitMix64(seed + i)
+        dims = tuple(r.randint(4, 24) for _ in range(3))
+        p = (3, 5, 7)[r.randint(0, 2)]
+        sigma = 0.05 + 0.15 * r.uniform()
+        centre = [r.uniform() for _ in range(3)]
+        ct = 2.0 * r.uniform() - 1.0
+        ph = 2.0 * math.pi * r.uniform()
+        st = math.sqrt(max(0.0, 1.0 - ct * ct))
+        mag = r.uniform()
+        vel = (mag * st * math.cos(ph), mag * st * math.sin(ph), mag * ct)
+        vsum = max(sum(abs(x) for x in vel), 1e-3)
+        dt = 0.1 * min(1.0 / d for d in dims) / ((2 * p + 1) * vsum)
+        members.append(dict(dims=dims, p=p, sigma=sigma, centre=centre, vel=vel, dt=dt))
+    return members
+
+
+def bench_ensemble(sdg, args):
+    import workloads as W
+    members = ensemble_workload(args.ens_n, args.seed + 1000)
+    ops = {p: sdg.operator_generate(p) for p in (3, 5, 7)}
+    t0 = time.perf_counter()
+    ens = sdg.Ensemble([m["dims"] for m in members], [m["p"] for m in members],
+                       [m["dt"] for m in members], ops)
+    for i, m in enumerate(members):
+        ens.init_blob(i, m["centre"], m["sigma"], m["vel"])
+    sdg.synchronize()
+    # initial states of a few members, for the FP64 comparison below
+    sample = list(range(0, args.ens_n, max(1, args.ens_n // 6)))[:6]
+    q0 = {i: ens.download(i) for i in sample}
+    cfg = ens.tune()
+    ens.step(args.warmup)
+    sdg.synchronize()
+    nst = args.ens_steps - args.warmup
+    ms = ens.step_timed(nst)
+    t = ms / 1e3
+    dof = ens.total_dofs
+    # the plain FP64 path on the same members (sequential solves), measured
+    # on the sample and scaled by DOF count
+    plain_t, plain_dof, errs, drift = 0.0, 0, [], []
+    for i in sample:
+        m = members[i]
+        x, D, Dt, L = ops[m["p"]]
+        s = sdg.Solver(*m["dims"], m["p"], D, L, precision=sdg.PREC_FP64)
+        n = q0[i].size
+        s.upload(q0[i], np.full(n, m["vel"][0]), np.full(n, m["vel"][1]), np.full(n, m["vel"][2]))
+        plain_t += s.step_timed(m["dt"], args.ens_steps) / 1e3
+        plain_dof += n
+        ref = s.download()
+        s.close()
+        got = ens.download(i)
+        # members ran warmup + timed = ens_steps steps
+        errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+        m0 = W.mass(q0[i], x, *m["dims"])
+        drift.append(abs(W.mass(got, x, *m["dims"]) - m0) / abs(m0))
+    ens.close()
+    per_solve = t / nst * args.ens_steps
+    plain_per_solve = plain_t / plain_dof * dof  # all members, sequentially
+    return {
+        "workload": f"{args.ens_n} instances, Ne per axis U{{4..24}}, p in {{3,5,7}}, "
+                    f"sigma U[0.05,0.2], constant |u|<=1, {args.ens_steps} steps, "
+                    "FP32 compute / FP64 RK state, one persistent launch per stage, CUDA graph",
+        "total_dof": dof,
+        "solves_per_s": args.ens_n / per_solve,
+        "gdof_updates_per_s": dof * 3 * nst / t / 1e9,
+        "hbm_frac": dof * 3 * nst * BYTES_PER_DOF_UPDATE["fp32"] / t / 1e9 / measured_peaks()[0],
+        "plain_fp64_solves_per_s": args.ens_n / plain_per_solve,
+        "ratio_vs_plain": plain_per_solve / per_solve,
+        "rel_l2_vs_fp64_max": max(errs), "mass_drift_max": max(drift),
+        "autotuned": cfg, "launches_per_step": 4,
+        "setup_s": time.perf_counter() - t0,
+    }
+
+
+def bench_serving(sdg, args):
+    """Poisson arrivals of solves (Ne per axis U{4..32}, p U{2..11}, nstep
+    U{10..500}, Gaussian tracer in a constant velocity, FP32 compute / FP64
+    state) into the continuous-batching server."""
+    import math
+    import workloads as W
+    ops = {p: sdg.operator_generate(p) for p in range(2, 12)}
+    rng = W.SplitMix64(args.seed + 5000)
+    reqs, arrivals, t = [], [], 0.0
+    for i in range(args.serve_n):
+        dims = tuple(rng.randint(4, args.serve_max_ne) for _ in range(3))
+        p = rng.randint(2, 11)
+        nstep = rng.randint(10, 500)
+        vel = (2 * rng.uniform() - 1, 2 * rng.uniform() - 1, 2 * rng.uniform() - 1)
+        dt = 0.1 * min(1.0 / d for d in dims) / ((2 * p + 1) * max(sum(abs(v) for v in vel), 1e-3))
+        reqs.append(dict(NeX=dims[0], NeY=dims[1], NeZ=dims[2], p=p, nstep=nstep, dt=dt,
+                         centre=[rng.uniform() for _ in range(3)],
+                         sigma=0.05 + 0.15 * rng.uniform(), velocity=vel))
+        t += -math.log(1.0 - rng.uniform()) / args.serve_rate
+        arrivals.append(t)
+    srv = sdg.Server(ops, hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)))
+    # warm the batched kernel and the pool
+    srv.wait(srv.submit(**reqs[0]))
+    srv.reset_stats()
+    tickets = []
+    t0 = time.perf_counter()
+    for r, ta in zip(reqs, arrivals):
+        now = time.perf_counter() - t0
+        if ta > now:
+            time.sleep(ta - now)
+        tickets.append(srv.submit(**r))
+    lat = [srv.wait(tk)[0]["latency_s"] for tk in tickets]
+    span = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    dofs = sum((r["p"] + 1) ** 3 * r["NeX"] * r["NeY"] * r["NeZ"] * 3 * r["nstep"] for r in reqs)
+    # the plain FP64 path on the first requests, one after the other
+    k = min(args.serve_plain_sample, len(reqs))
+    pt = 0.0
+    for r in reqs[:k]:
+        x, D, Dt, L = ops[r["p"]]
+        s = sdg.Solver(r["NeX"], r["NeY"], r["NeZ"], r["p"], D, L, precision=sdg.PREC_FP64)
+        n = (r["p"] + 1) ** 3 * r["NeX"] * r["NeY"] * r["NeZ"]
+        # the work per step does not depend on the values: a zero tracer
+        s.upload(np.zeros(n), np.full(n, r["velocity"][0]), np.full(n, r["velocity"][1]),
+                 np.full(n, r["velocity"][2]))
+        sdg.synchronize()
+        tt = time.perf_counter()
+        s.step(r["dt"], r["nstep"])
+        sdg.synchronize()
+        pt += time.perf_counter() - tt
+        s.close()
+    sample_dofs = sum((r["p"] + 1) ** 3 * r["NeX"] * r["NeY"] * r["NeZ"] * 3 * r["nstep"]
+                      for r in reqs[:k])
+    plain_solves = len(reqs) / (pt * dofs / sample_dofs)
+    return {
+        "workload": f"{args.serve_n} requests, Poisson arrivals at {args.serve_rate} req/s, "
+                    f"Ne per axis U{{4..{args.serve_max_ne}}}, p U{{2..11}}, nstep U{{10..500}}, "
+                    "FP32 compute / FP64 state, admission by HBM budget",
+        "offered_rate_req_s": args.serve_rate,
+        "solves_per_s": len(reqs) / span,
+        "p50_latency_s": float(np.percentile(lat, 50)),
+        "p99_latency_s": float(np.percentile(lat, 99)),
+        "gdof_updates_per_s": dofs / span / 1e9,
+        "plain_fp64_solves_per_s_same_requests": plain_solves,
+        "ratio_vs_plain": (len(reqs) / span) / plain_solves,
+        "server": {k2: st[k2] for k2 in ("completed", "steps_run", "launches", "fatal_status")},
+    }
+
+
 def run_ours(args, ws, rank, local):
     import sdg
     if sdg.device_count() < 1:
@@ -395,6 +547,10 @@ def run_ours(args, ws, rank, local):
     }
     if other is not None:
         line["fp64_emulated"] = other
+    if ws == 1 and not args.no_ensemble:
+        line["ensemble"] = bench_ensemble(sdg, args)
+    if ws == 1 and not args.no_serving:
+        line["serving"] = bench_serving(sdg, args)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -417,6 +573,15 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-emu", action="store_true",
                     help="skip the emulated-FP64 measurement beside the FP64 headline")
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--ens-n", type=int, default=256)
+    ap.add_argument("--ens-steps", type=int, default=100)
+    ap.add_argument("--serve-n", type=int, default=60)
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-max-ne", type=int, default=32)
+    ap.add_argument("--serve-budget-gb", type=float, default=64.0)
+    ap.add_argument("--serve-plain-sample", type=int, default=8)
     ap.add_argument("--no-microbench", action="store_true",
                     help="skip the live DFMA/FFMA peak measurement")
     args = ap.parse_args()

@@ -241,6 +241,102 @@ int sdg_solver_launches_per_step(const sdg_solver* s);
 void* sdg_solver_stream(const sdg_solver* s);
 int sdg_solver_destroy(sdg_solver* s);
 
+/* ---- batched ensembles: one persistent launch per RK stage ------------- */
+
+/* Many independent periodic boxes (orders 1..11, any sizes, each with its own
+ * dt) advanced together in FP32-compute / FP64-state form.  A step is a CUDA
+ * graph of four kernels: three persistent stage launches that each cover
+ * every instance (blocks pull (instance, element block) work items from a
+ * counter and dispatch on the instance's order) and an index advance.
+ * dims holds NeX,NeY,NeZ per instance; D1D_by_order / Lift_by_order /
+ * x1D_by_order are indexed by the order (entries for absent orders may be
+ * NULL; x1D_by_order may be NULL when sdg_ensemble_init_blob is not used).
+ * There is no reference counterpart: the reference advances one box. */
+typedef struct sdg_ensemble sdg_ensemble;
+int sdg_ensemble_create(sdg_ensemble** out, int n, const int* dims,
+                        const int* orders, const double* dt,
+                        const double* const* D1D_by_order,
+                        const double* const* Lift_by_order,
+                        const double* const* x1D_by_order, void* stream);
+/* Owned q,u,v,w of instance i (Np*Ne values each, host memory). */
+int sdg_ensemble_upload(sdg_ensemble* e, int i, const double* q,
+                        const double* u, const double* v, const double* w);
+/* Device-side initial condition of instance i: Gaussian tracer of width
+ * sigma around centre[3] (periodic unit box) in the constant velocity[3]. */
+int sdg_ensemble_init_blob(sdg_ensemble* e, int i, const double* centre,
+                           double sigma, const double* velocity);
+/* Autotuner: picks elements per block for every order present and the block
+ * size by timing stage launches on this ensemble; leaves the state as is. */
+int sdg_ensemble_tune(sdg_ensemble* e);
+int sdg_ensemble_set_epb(sdg_ensemble* e, int p, int epb);
+int sdg_ensemble_set_threads(sdg_ensemble* e, int threads);
+/* epb_by_order receives 12 entries (index = order). */
+int sdg_ensemble_get_config(const sdg_ensemble* e, int* epb_by_order,
+                            int* threads, int* grid);
+int sdg_ensemble_step(sdg_ensemble* e, int nstep);
+int sdg_ensemble_step_timed(sdg_ensemble* e, int nstep, double* ms);
+int sdg_ensemble_download(sdg_ensemble* e, int i, double* q);
+long long sdg_ensemble_total_dofs(const sdg_ensemble* e);
+int sdg_ensemble_launches_per_step(const sdg_ensemble* e);
+int sdg_ensemble_destroy(sdg_ensemble* e);
+
+/* ---- serving: continuous batching of advection solves ------------------ */
+
+/* A scheduler thread owns the device.  Requests (a periodic box with its own
+ * order 1..11, size, dt and step count, and a Gaussian tracer in a constant
+ * velocity generated on the device) are admitted while the HBM budget and the
+ * slot count allow; every active request advances one SSP-RK3 step per
+ * round of batched persistent launches (FP32 compute, FP64 state), so
+ * requests that arrive while others run share the GPU from their next step
+ * on.  Finished requests release their memory at once.  No reference
+ * counterpart: the reference runs one box per process. */
+typedef struct sdg_server sdg_server;
+typedef struct {
+  int device;               /* CUDA device the server runs on */
+  size_t hbm_budget_bytes;  /* admission limit for request state (clamped to
+                               90% of the device's free memory) */
+  int max_active;           /* requests advanced together at most */
+  int max_window_steps;     /* steps between admission points (default 8) */
+  int threads;              /* block size of the batched kernel (0: 256) */
+  int epb_by_order[16];     /* elements per block by order (0: default) */
+} sdg_server_config;
+typedef struct {
+  int NeX, NeY, NeZ, p, nstep;
+  double dt;
+  double centre[3];         /* Gaussian tracer centre in [0,1)^3 */
+  double sigma;             /* Gaussian width */
+  double velocity[3];       /* constant velocity */
+} sdg_request;
+typedef struct {
+  int status;               /* SDG_OK or the error that ended the request */
+  double latency_s;         /* finish - submit */
+  double queue_s;           /* admit - submit */
+  long long dofs;
+} sdg_result;
+typedef struct {
+  long long completed, steps_run, launches;
+  double dof_updates;
+  size_t bytes_in_use;
+  int active, pending;
+  double p50_latency_s, p99_latency_s;
+  double span_s;            /* first submit to last finish */
+  int fatal_status;
+} sdg_server_stats;
+int sdg_server_create(sdg_server** out, const sdg_server_config* cfg,
+                      const double* const* D1D_by_order,
+                      const double* const* Lift_by_order,
+                      const double* const* x1D_by_order);
+/* Thread-safe.  out_state (Np*Ne doubles, may be NULL) receives the final
+ * state; it must stay valid until sdg_server_wait returns. */
+int sdg_server_submit(sdg_server* s, const sdg_request* r, double* out_state,
+                      uint64_t* ticket);
+/* Blocks until the request finishes (SDG_ERR_TIMEOUT after timeout_s). */
+int sdg_server_wait(sdg_server* s, uint64_t ticket, double timeout_s,
+                    sdg_result* res);
+int sdg_server_get_stats(sdg_server* s, sdg_server_stats* out);
+int sdg_server_reset_stats(sdg_server* s);
+int sdg_server_destroy(sdg_server* s);
+
 /* ---- measurement helpers ----------------------------------------------- */
 
 /* Device memory for callers of the *_dev entry points that have no CUDA

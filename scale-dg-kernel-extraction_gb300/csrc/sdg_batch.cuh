@@ -1,0 +1,58 @@
+// Batched advance of many independent boxes (an ensemble, or the requests a
+// server holds) in ONE persistent launch per RK stage.
+//
+// Every box is an instance with its own order p, size, dt, rotating state
+// buffers and velocity.  A work item is one block's worth of consecutive
+// elements of one instance.  The persistent kernel's blocks pull items from a
+// global counter, resolve the instance's buffers for the stage, and run the
+// same fused stage body as the single-box solver (stage_block, FP32 compute,
+// FP64 state), dispatched on the instance's order.  Each instance's current
+// buffer index lives on the device and is advanced by a tiny kernel after
+// stage 3, so one captured CUDA graph replays every step.
+#pragma once
+
+#include "sdg_stage.cuh"
+
+namespace sdg {
+
+constexpr int kBatchMaxOrder = 11;  // orders the batched kernel compiles
+constexpr int kBatchThreadsMax = 512;
+
+struct BatchInst {
+  double* q[3];        // rotating FP64 state buffers
+  const float* u;      // FP32 velocity
+  const float* v;
+  const float* w;
+  const float* D;      // FP32 D1D(Nq,Nq) of this order
+  const float* Lift;   // FP32 Lift_mat of this order
+  Box box;
+  double dt;
+  int p;
+  int cur;             // buffer holding the current state
+  int active;          // 0: skipped by the stage kernel and by the advance
+};
+
+struct BatchItem {
+  int inst;
+  int e_begin;
+  int e_count;
+};
+
+// Launches one stage over `n_items` items; counter must be zero on entry.
+int batch_stage_launch(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,
+                       int* d_counter, int grid, int threads, size_t smem, cudaStream_t st);
+// cur = (cur + 1) % 3 for every active instance.
+int batch_advance_launch(BatchInst* d_inst, int n_inst, cudaStream_t st);
+// Dynamic shared memory the kernel needs for `epb` elements of order p.
+size_t batch_smem_bytes(int p, int epb);
+// Resident blocks of the batch kernel per SM for a block size and smem size.
+int batch_blocks_per_sm(int threads, size_t smem);
+int batch_set_max_smem(size_t smem);
+
+// Device-side initial condition: Gaussian tracer exp(-d^2/(2 sigma^2)) around
+// `centre` (periodic minimum image on the unit box) and a constant velocity,
+// written into an instance's current state buffer and velocity arrays.
+int batch_init_blob(const BatchInst& inst, const double* d_x1D, const double centre[3],
+                    double sigma, const double vel[3], cudaStream_t st);
+
+}  // namespace sdg

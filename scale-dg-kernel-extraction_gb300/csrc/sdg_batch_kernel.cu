@@ -1,0 +1,173 @@
+// The persistent batched stage kernel and its helpers (see sdg_batch.cuh).
+#include "sdg_batch.cuh"
+
+namespace sdg {
+
+namespace {
+
+// SSP-RK3 coefficients, mod_common.f90:28-30
+__constant__ double c_rk_a[3] = {0.0, 0.75, 1.0 / 3.0};
+__constant__ double c_rk_b[3] = {1.0, 0.25, 2.0 / 3.0};
+
+template <int P>
+__device__ __forceinline__ void run_order(const StageArgs& a, const BatchItem& w,
+                                          unsigned char* smem) {
+  stage_block<P, float, float, false>(a, w.e_begin, w.e_count, smem);
+}
+
+__global__ void __launch_bounds__(kBatchThreadsMax)
+    batch_stage_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
+                       int n_items, int stage, int* counter) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= n_items) return;  // uniform across the block
+    const BatchItem w = items[it];
+    const BatchInst& I = insts[w.inst];
+    if (I.active) {
+      const int s0 = I.cur, s1 = (s0 + 1) % 3, s2 = (s0 + 2) % 3;
+      StageArgs a;
+      a.q_in = (stage == 0) ? I.q[s0] : (stage == 1) ? I.q[s1] : I.q[s2];
+      a.q0 = (stage == 0) ? nullptr : I.q[s0];
+      a.q_out = (stage == 1) ? I.q[s2] : I.q[s1];
+      a.u = I.u;
+      a.v = I.v;
+      a.w = I.w;
+      a.D = I.D;
+      a.Lift = I.Lift;
+      a.box = I.box;
+      a.elem_begin = 0;
+      a.elem_count = I.box.Ne;
+      a.a = c_rk_a[stage];
+      a.b = c_rk_b[stage];
+      a.dt = I.dt;
+      a.cdt_hi = 0.0f;
+      a.cdt_lo = 0.0f;
+      a.tend_only = 0;
+      switch (I.p) {
+        case 1: run_order<1>(a, w, smem); break;
+        case 2: run_order<2>(a, w, smem); break;
+        case 3: run_order<3>(a, w, smem); break;
+        case 4: run_order<4>(a, w, smem); break;
+        case 5: run_order<5>(a, w, smem); break;
+        case 6: run_order<6>(a, w, smem); break;
+        case 7: run_order<7>(a, w, smem); break;
+        case 8: run_order<8>(a, w, smem); break;
+        case 9: run_order<9>(a, w, smem); break;
+        case 10: run_order<10>(a, w, smem); break;
+        case 11: run_order<11>(a, w, smem); break;
+        default: break;
+      }
+    }
+    __syncthreads();  // the next item reuses shared memory and s_item
+  }
+}
+
+__global__ void batch_advance_kernel(BatchInst* insts, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && insts[i].active) insts[i].cur = (insts[i].cur + 1) % 3;
+}
+
+__global__ void init_blob_kernel(double* q, float* u, float* v, float* w, const double* x1D,
+                                 Box box, int nq, double cx, double cy, double cz,
+                                 double inv2s2, float ux, float uy, float uz) {
+  const long long np = (long long)nq * nq * nq;
+  const long long total = np * box.Ne;
+  const double dx = 2.0 / box.Es[0], dy = 2.0 / box.Es[1], dz = 2.0 / box.Es[2];
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const long long e = g / np;
+    const int n = (int)(g - e * np);
+    const int i = n % nq, j = (n / nq) % nq, k = n / (nq * nq);
+    const int ex = (int)(e % box.NeX);
+    const int ey = (int)((e / box.NeX) % box.NeY);
+    const int ez = (int)(e / ((long long)box.NeX * box.NeY));
+    // node position as mesh_setup places it (mod_mesh.f90:141-145, :344-347)
+    const double x = (ex + 0.5) * dx + 0.5 * dx * x1D[i];
+    const double y = (ey + 0.5) * dy + 0.5 * dy * x1D[j];
+    const double z = (ez + 0.5) * dz + 0.5 * dz * x1D[k];
+    double ddx = x - cx, ddy = y - cy, ddz = z - cz;
+    ddx -= rint(ddx);
+    ddy -= rint(ddy);
+    ddz -= rint(ddz);
+    q[g] = exp(-(ddx * ddx + ddy * ddy + ddz * ddz) * inv2s2);
+    u[g] = ux;
+    v[g] = uy;
+    w[g] = uz;
+  }
+}
+
+template <int P>
+size_t smem_for(int epb) {
+  return stage_block_smem<P, float>(epb);
+}
+
+}  // namespace
+
+size_t batch_smem_bytes(int p, int epb) {
+  switch (p) {
+    case 1: return smem_for<1>(epb);
+    case 2: return smem_for<2>(epb);
+    case 3: return smem_for<3>(epb);
+    case 4: return smem_for<4>(epb);
+    case 5: return smem_for<5>(epb);
+    case 6: return smem_for<6>(epb);
+    case 7: return smem_for<7>(epb);
+    case 8: return smem_for<8>(epb);
+    case 9: return smem_for<9>(epb);
+    case 10: return smem_for<10>(epb);
+    case 11: return smem_for<11>(epb);
+    default: return 0;
+  }
+}
+
+int batch_set_max_smem(size_t smem) {
+  SDG_CUDA_TRY(cudaFuncSetAttribute(batch_stage_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  return SDG_OK;
+}
+
+int batch_blocks_per_sm(int threads, size_t smem) {
+  int nb = 0;
+  if (batch_set_max_smem(smem) != SDG_OK) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel, threads, smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return nb;
+}
+
+int batch_stage_launch(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,
+                       int* d_counter, int grid, int threads, size_t smem, cudaStream_t st) {
+  if (n_items <= 0) return SDG_OK;
+  batch_stage_kernel<<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage, d_counter);
+  SDG_CUDA_TRY(cudaGetLastError());
+  return SDG_OK;
+}
+
+int batch_advance_launch(BatchInst* d_inst, int n_inst, cudaStream_t st) {
+  if (n_inst <= 0) return SDG_OK;
+  batch_advance_kernel<<<(n_inst + 255) / 256, 256, 0, st>>>(d_inst, n_inst);
+  SDG_CUDA_TRY(cudaGetLastError());
+  return SDG_OK;
+}
+
+int batch_init_blob(const BatchInst& inst, const double* d_x1D, const double centre[3],
+                    double sigma, const double vel[3], cudaStream_t st) {
+  const int nq = inst.p + 1;
+  const long long total = (long long)nq * nq * nq * inst.box.Ne;
+  long long nb = (total + 255) / 256;
+  if (nb > 152LL * 32) nb = 152LL * 32;
+  init_blob_kernel<<<(unsigned)(nb > 0 ? nb : 1), 256, 0, st>>>(
+      inst.q[inst.cur], const_cast<float*>(inst.u), const_cast<float*>(inst.v),
+      const_cast<float*>(inst.w), d_x1D, inst.box, nq, centre[0], centre[1], centre[2],
+      1.0 / (2.0 * sigma * sigma), (float)vel[0], (float)vel[1], (float)vel[2]);
+  SDG_CUDA_TRY(cudaGetLastError());
+  return SDG_OK;
+}
+
+}  // namespace sdg

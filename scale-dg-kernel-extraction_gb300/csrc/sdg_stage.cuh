@@ -129,32 +129,31 @@ __device__ __forceinline__ long long neighbor(const Box& b, long long e, int f) 
 template <typename T> __device__ __forceinline__ T to_ct(double x) { return (T)x; }
 template <typename T> __device__ __forceinline__ T to_ct(float x) { return (T)x; }
 
-template <int P, typename CT, typename VT, bool SPLIT3>
-constexpr size_t stage_smem_bytes() {
+
+// Dynamic shared memory of one block holding `nloc` elements of order P.
+template <int P, typename CT>
+__host__ __device__ constexpr size_t stage_block_smem(int nloc) {
   using O = Ord<P>;
-  using C = StageCfg<P, CT>;
-  return sizeof(CT) * (size_t)(O::NQ2 + C::EPB * (4 * O::NP + O::NFT));
+  return sizeof(CT) * (size_t)(O::NQ2 + nloc * (4 * O::NP + O::NFT));
 }
 
+// One block advances elements [eb, eb + nloc) of the box in `a` through one
+// stage.  The block size and nloc are runtime values, so the batched
+// persistent kernel can run any order and any elements-per-block choice
+// through the same body; `smem` holds stage_block_smem<P, CT>(nloc) bytes.
 template <int P, typename CT, typename VT, bool SPLIT3>
-__global__ void __launch_bounds__(StageCfg<P, CT>::THREADS)
-    stage_kernel(const StageArgs a) {
+__device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, int nloc,
+                                            unsigned char* smem) {
   using O = Ord<P>;
-  using C = StageCfg<P, CT>;
-  constexpr int NQ = O::NQ, NQ2 = O::NQ2, NP = O::NP, NFP = O::NFP,
-                NFT = O::NFT, EPB = C::EPB, T = C::THREADS;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  CT* sD = reinterpret_cast<CT*>(smem_raw);
+  constexpr int NQ = O::NQ, NQ2 = O::NQ2, NP = O::NP, NFP = O::NFP, NFT = O::NFT;
+  const int T = blockDim.x;
+  CT* sD = reinterpret_cast<CT*>(smem);
   CT* sq = sD + NQ2;
-  CT* su = sq + EPB * NP;
-  CT* sv = su + EPB * NP;
-  CT* sw = sv + EPB * NP;
-  CT* sf = sw + EPB * NP;
+  CT* su = sq + nloc * NP;
+  CT* sv = su + nloc * NP;
+  CT* sw = sv + nloc * NP;
+  CT* sf = sw + nloc * NP;
 
-  const long long eb = a.elem_begin + (long long)blockIdx.x * EPB;
-  const long long eend = a.elem_begin + a.elem_count;
-  const int nloc = (int)((eend - eb) < EPB ? (eend - eb) : EPB);
-  if (nloc <= 0) return;
   const double* __restrict__ qin = a.q_in;
   const VT* __restrict__ gu = static_cast<const VT*>(a.u);
   const VT* __restrict__ gv = static_cast<const VT*>(a.v);
@@ -232,6 +231,23 @@ __global__ void __launch_bounds__(StageCfg<P, CT>::THREADS)
       a.q_out[g] = r;
     }
   }
+}
+
+template <int P, typename CT, typename VT, bool SPLIT3>
+constexpr size_t stage_smem_bytes() {
+  return stage_block_smem<P, CT>(StageCfg<P, CT>::EPB);
+}
+
+template <int P, typename CT, typename VT, bool SPLIT3>
+__global__ void __launch_bounds__(StageCfg<P, CT>::THREADS)
+    stage_kernel(const StageArgs a) {
+  constexpr int EPB = StageCfg<P, CT>::EPB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const long long eb = a.elem_begin + (long long)blockIdx.x * EPB;
+  const long long eend = a.elem_begin + a.elem_count;
+  const int nloc = (int)((eend - eb) < EPB ? (eend - eb) : EPB);
+  if (nloc <= 0) return;
+  stage_block<P, CT, VT, SPLIT3>(a, eb, nloc, smem_raw);
 }
 
 template <int P, typename CT, typename VT, bool SPLIT3>

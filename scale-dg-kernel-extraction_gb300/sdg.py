@@ -37,6 +37,31 @@ PREC_FP64 = 0
 PREC_FP32 = 1
 PREC_FP64_EMU = 2
 
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_size_t), ("max_active", C.c_int),
+                ("max_window_steps", C.c_int), ("threads", C.c_int),
+                ("epb_by_order", C.c_int * 16)]
+
+
+class Request(C.Structure):
+    _fields_ = [("NeX", C.c_int), ("NeY", C.c_int), ("NeZ", C.c_int), ("p", C.c_int),
+                ("nstep", C.c_int), ("dt", C.c_double), ("centre", C.c_double * 3),
+                ("sigma", C.c_double), ("velocity", C.c_double * 3)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int), ("latency_s", C.c_double), ("queue_s", C.c_double),
+                ("dofs", C.c_longlong)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_longlong), ("steps_run", C.c_longlong),
+                ("launches", C.c_longlong), ("dof_updates", C.c_double),
+                ("bytes_in_use", C.c_size_t), ("active", C.c_int), ("pending", C.c_int),
+                ("p50_latency_s", C.c_double), ("p99_latency_s", C.c_double),
+                ("span_s", C.c_double), ("fatal_status", C.c_int)]
+
+
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _vp = C.c_void_p
@@ -97,6 +122,27 @@ def _load() -> C.CDLL:
         "sdg_pinned_alloc": ([C.c_size_t, C.POINTER(_vp)], _i),
         "sdg_pinned_free": ([_vp], _i),
         "sdg_microbench_peaks": ([C.POINTER(_d)] * 4, _i),
+        "sdg_ensemble_create": ([C.POINTER(_vp), _i, _ip, _ip, _dp, C.POINTER(_vp),
+                                 C.POINTER(_vp), C.POINTER(_vp), _vp], _i),
+        "sdg_ensemble_upload": ([_vp, _i, _dp, _dp, _dp, _dp], _i),
+        "sdg_ensemble_init_blob": ([_vp, _i, _dp, _d, _dp], _i),
+        "sdg_ensemble_tune": ([_vp], _i),
+        "sdg_ensemble_set_epb": ([_vp, _i, _i], _i),
+        "sdg_ensemble_set_threads": ([_vp, _i], _i),
+        "sdg_ensemble_get_config": ([_vp, _ip, C.POINTER(_i), C.POINTER(_i)], _i),
+        "sdg_ensemble_step": ([_vp, _i], _i),
+        "sdg_ensemble_step_timed": ([_vp, _i, C.POINTER(_d)], _i),
+        "sdg_ensemble_download": ([_vp, _i, _dp], _i),
+        "sdg_ensemble_total_dofs": ([_vp], C.c_longlong),
+        "sdg_ensemble_launches_per_step": ([_vp], _i),
+        "sdg_ensemble_destroy": ([_vp], _i),
+        "sdg_server_create": ([C.POINTER(_vp), C.POINTER(ServerConfig), C.POINTER(_vp),
+                               C.POINTER(_vp), C.POINTER(_vp)], _i),
+        "sdg_server_submit": ([_vp, C.POINTER(Request), _vp, C.POINTER(C.c_uint64)], _i),
+        "sdg_server_wait": ([_vp, C.c_uint64, _d, C.POINTER(Result)], _i),
+        "sdg_server_get_stats": ([_vp, C.POINTER(ServerStats)], _i),
+        "sdg_server_reset_stats": ([_vp], _i),
+        "sdg_server_destroy": ([_vp], _i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -341,6 +387,163 @@ class Solver:
     def close(self) -> None:
         if self._h is not None and self._h.value:
             lib.sdg_solver_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Ensemble:
+    """Independent boxes advanced together, one persistent launch per RK stage
+    (sdg_ensemble_* in include/sdg_advect.h); FP32 compute, FP64 state."""
+
+    def __init__(self, dims, orders, dt, ops_by_order, stream=None):
+        """dims: list of (NeX,NeY,NeZ); orders: list of p; dt: list;
+        ops_by_order: {p: (x1D, D1D, D1D_tr, Lift)}."""
+        n = len(orders)
+        self.n = n
+        self.orders = [int(p) for p in orders]
+        self.dims = [tuple(int(x) for x in d) for d in dims]
+        self._keep = ops_by_order
+        arrs = {p: [np.ascontiguousarray(a, dtype=np.float64) for a in v]
+                for p, v in ops_by_order.items()}
+        self._arrs = arrs
+        Dp = (_vp * 16)()
+        Lp = (_vp * 16)()
+        Xp = (_vp * 16)()
+        for p, (x, D, Dt, L) in arrs.items():
+            Dp[p] = D.ctypes.data
+            Lp[p] = L.ctypes.data
+            Xp[p] = x.ctypes.data
+        self._h = _vp()
+        _check(lib.sdg_ensemble_create(C.byref(self._h), n,
+                                       np.ascontiguousarray(np.array(dims, dtype=np.int32).reshape(-1)),
+                                       np.ascontiguousarray(np.array(orders, dtype=np.int32)),
+                                       np.ascontiguousarray(np.array(dt, dtype=np.float64)),
+                                       C.cast(Dp, C.POINTER(_vp)), C.cast(Lp, C.POINTER(_vp)),
+                                       C.cast(Xp, C.POINTER(_vp)), stream),
+               "sdg_ensemble_create")
+
+    def ndof(self, i) -> int:
+        nx, ny, nz = self.dims[i]
+        return (self.orders[i] + 1) ** 3 * nx * ny * nz
+
+    def upload(self, i, q, u, v, w) -> None:
+        _check(lib.sdg_ensemble_upload(self._h, i, _f64(q), _f64(u), _f64(v), _f64(w)),
+               "sdg_ensemble_upload")
+
+    def init_blob(self, i, centre, sigma, velocity) -> None:
+        _check(lib.sdg_ensemble_init_blob(self._h, i, _f64(centre), float(sigma),
+                                          _f64(velocity)), "sdg_ensemble_init_blob")
+
+    def tune(self) -> dict:
+        _check(lib.sdg_ensemble_tune(self._h), "sdg_ensemble_tune")
+        return self.config()
+
+    def set_epb(self, p, epb) -> None:
+        _check(lib.sdg_ensemble_set_epb(self._h, p, epb), "sdg_ensemble_set_epb")
+
+    def set_threads(self, threads) -> None:
+        _check(lib.sdg_ensemble_set_threads(self._h, threads), "sdg_ensemble_set_threads")
+
+    def config(self) -> dict:
+        epb = np.zeros(12, dtype=np.int32)
+        th, gr = _i(), _i()
+        _check(lib.sdg_ensemble_get_config(self._h, epb, C.byref(th), C.byref(gr)),
+               "sdg_ensemble_get_config")
+        return {"epb": {p: int(epb[p]) for p in sorted(set(self.orders))},
+                "threads": th.value, "grid": gr.value}
+
+    def step(self, nstep: int) -> None:
+        _check(lib.sdg_ensemble_step(self._h, int(nstep)), "sdg_ensemble_step")
+
+    def step_timed(self, nstep: int) -> float:
+        ms = _d()
+        _check(lib.sdg_ensemble_step_timed(self._h, int(nstep), C.byref(ms)),
+               "sdg_ensemble_step_timed")
+        return ms.value
+
+    def download(self, i) -> np.ndarray:
+        out = np.zeros(self.ndof(i))
+        _check(lib.sdg_ensemble_download(self._h, i, out), "sdg_ensemble_download")
+        return out
+
+    @property
+    def total_dofs(self) -> int:
+        return lib.sdg_ensemble_total_dofs(self._h)
+
+    def close(self) -> None:
+        if self._h is not None and self._h.value:
+            lib.sdg_ensemble_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _order_table(ops_by_order):
+    arrs = {p: [np.ascontiguousarray(a, dtype=np.float64) for a in v]
+            for p, v in ops_by_order.items()}
+    D, L, X = (_vp * 16)(), (_vp * 16)(), (_vp * 16)()
+    for p, (x, d, dt, lift) in arrs.items():
+        D[p], L[p], X[p] = d.ctypes.data, lift.ctypes.data, x.ctypes.data
+    return arrs, D, L, X
+
+
+class Server:
+    """Continuous-batching solve server (sdg_server_* in include/sdg_advect.h)."""
+
+    def __init__(self, ops_by_order, hbm_budget_bytes=64 << 30, max_active=512,
+                 max_window_steps=8, threads=0, device=0):
+        self._arrs, D, L, X = _order_table(ops_by_order)
+        cfg = ServerConfig()
+        cfg.device = device
+        cfg.hbm_budget_bytes = int(hbm_budget_bytes)
+        cfg.max_active = max_active
+        cfg.max_window_steps = max_window_steps
+        cfg.threads = threads
+        self._h = _vp()
+        _check(lib.sdg_server_create(C.byref(self._h), C.byref(cfg), C.cast(D, C.POINTER(_vp)),
+                                     C.cast(L, C.POINTER(_vp)), C.cast(X, C.POINTER(_vp))),
+               "sdg_server_create")
+        self._outs = {}
+
+    def submit(self, NeX, NeY, NeZ, p, nstep, dt, centre, sigma, velocity, want_state=False):
+        r = Request(NeX, NeY, NeZ, p, nstep, dt, (C.c_double * 3)(*centre), sigma,
+                    (C.c_double * 3)(*velocity))
+        out = np.zeros((p + 1) ** 3 * NeX * NeY * NeZ) if want_state else None
+        t = C.c_uint64()
+        _check(lib.sdg_server_submit(self._h, C.byref(r), out.ctypes.data if out is not None
+                                     else None, C.byref(t)), "sdg_server_submit")
+        self._outs[t.value] = out
+        return t.value
+
+    def wait(self, ticket, timeout_s=600.0):
+        """Returns (result dict, final state or None)."""
+        res = Result()
+        st = lib.sdg_server_wait(self._h, ticket, float(timeout_s), C.byref(res))
+        out = self._outs.pop(ticket, None) if st != ERR_TIMEOUT else self._outs.get(ticket)
+        _check(st, "sdg_server_wait")
+        return ({"status": res.status, "latency_s": res.latency_s, "queue_s": res.queue_s,
+                 "dofs": res.dofs}, out)
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        _check(lib.sdg_server_get_stats(self._h, C.byref(s)), "sdg_server_get_stats")
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def reset_stats(self) -> None:
+        _check(lib.sdg_server_reset_stats(self._h), "sdg_server_reset_stats")
+
+    def close(self) -> None:
+        if self._h is not None and self._h.value:
+            lib.sdg_server_destroy(self._h)
         self._h = None
 
     def __del__(self):

@@ -1,0 +1,104 @@
+"""GPU tests of the batched ensemble (one persistent launch per RK stage over
+all instances, CUDA graph per step): every member must equal the standalone
+FP32-compute solver bit for bit, stay within the FP32-form tolerance of the
+FP64 oracle, and keep those results after the autotuner changes the launch
+shape."""
+import numpy as np
+import pytest
+
+import sdg
+import workloads as W
+from helpers import TOL_FP32, Case, operators, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+MEMBERS = [((3, 2, 4), 3), ((2, 2, 2), 7), ((4, 4, 1), 1), ((1, 3, 2), 5), ((2, 1, 2), 11),
+           ((3, 3, 3), 2), ((2, 2, 3), 9), ((5, 2, 2), 3)]
+
+
+def build(members, seed0=100):
+    ops = {p: operators(p) for _, p in members}
+    fields, dts = [], []
+    for i, (dims, p) in enumerate(members):
+        q, u, v, w = W.blob(*dims, ops[p][0], W.BASE_SEED + seed0 + i)
+        fields.append((q, u, v, w))
+        dts.append(W.cfl_dt(*dims, p, u, v, w))
+    ens = sdg.Ensemble([d for d, _ in members], [p for _, p in members], dts, ops)
+    for i, f in enumerate(fields):
+        ens.upload(i, *f)
+    return ens, fields, dts, ops
+
+
+def standalone(dims, p, fields, dt, ops, nstep):
+    s = sdg.Solver(*dims, p, ops[p][1], ops[p][3], opt=sdg.OPT_GENERAL, precision=sdg.PREC_FP32)
+    s.upload(*fields)
+    s.step(dt, nstep)
+    return s.download()
+
+
+def test_members_equal_the_standalone_fp32_solver_bitwise():
+    ens, fields, dts, ops = build(MEMBERS)
+    ens.step(4)
+    for i, (dims, p) in enumerate(MEMBERS):
+        want = standalone(dims, p, fields[i], dts[i], ops, 4)
+        assert np.array_equal(ens.download(i), want), (i, dims, p)
+
+
+def test_members_within_fp32_tolerance_of_fp64_oracle():
+    members = MEMBERS[:4]
+    ens, fields, dts, ops = build(members, seed0=200)
+    ens.step(10)
+    for i, (dims, p) in enumerate(members):
+        c = Case(*dims, p, ic="blob", seed=W.BASE_SEED + 200 + i, ops=ops[p])
+        c.dt = dts[i]
+        assert rel_l2(ens.download(i), c.oracle_run(10)) <= TOL_FP32
+
+
+def test_autotuner_keeps_results_and_picks_valid_shapes():
+    ens, fields, dts, ops = build(MEMBERS, seed0=300)
+    cfg = ens.tune()
+    assert cfg["threads"] in (128, 256, 512) and cfg["grid"] > 0
+    for p, e in cfg["epb"].items():
+        assert e >= 1
+    ens.step(3)
+    for i, (dims, p) in enumerate(MEMBERS):
+        want = standalone(dims, p, fields[i], dts[i], ops, 3)
+        assert np.array_equal(ens.download(i), want)
+
+
+def test_explicit_shapes_and_graph_replay_compose():
+    ens, fields, dts, ops = build(MEMBERS[:3], seed0=400)
+    ens.set_threads(128)
+    ens.set_epb(3, 1)
+    ens.step(2)
+    ens.set_epb(3, 4)
+    ens.step(3)
+    for i, (dims, p) in enumerate(MEMBERS[:3]):
+        want = standalone(dims, p, fields[i], dts[i], ops, 5)
+        assert np.array_equal(ens.download(i), want)
+
+
+def test_device_initial_condition_matches_host_recipe():
+    dims, p = (3, 2, 2), 4
+    ops = {p: operators(p)}
+    ens = sdg.Ensemble([dims], [p], [1e-3], ops)
+    centre, sigma, vel = (0.3, 0.7, 0.55), 0.12, (0.4, -0.2, 0.1)
+    ens.init_blob(0, centre, sigma, vel)
+    X, Y, Z = W.node_coords(*dims, ops[p][0])
+
+    def mi(d):
+        return d - np.round(d)
+
+    q = np.exp(-(mi(X - centre[0]) ** 2 + mi(Y - centre[1]) ** 2 + mi(Z - centre[2]) ** 2)
+               / (2 * sigma * sigma))
+    assert rel_l2(ens.download(0), q) < 1e-13
+
+
+def test_bad_ensemble_arguments_are_rejected():
+    ops = {3: operators(3)}
+    with pytest.raises(sdg.SdgError) as e:
+        sdg.Ensemble([(2, 2, 2)], [12], [1e-3], {12: operators(12)})
+    assert e.value.status == sdg.ERR_UNSUPPORTED_ORDER
+    with pytest.raises(sdg.SdgError) as e:
+        sdg.Ensemble([(2, 0, 2)], [3], [1e-3], ops)
+    assert e.value.status == sdg.ERR_INVALID_ARG

@@ -1,0 +1,100 @@
+"""GPU tests of the continuous-batching server: a request's result is the same
+alone and in a mix of requests that arrive while it runs, admission respects
+the HBM budget, and waits are bounded on the host."""
+import time
+
+import numpy as np
+import pytest
+
+import sdg
+import workloads as W
+from helpers import TOL_FP32, Case, operators, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+ORDERS = (2, 3, 5, 7, 11)
+
+
+@pytest.fixture(scope="module")
+def ops():
+    return {p: operators(p) for p in ORDERS}
+
+
+def req(dims, p, nstep, seed):
+    prm = W.blob_params(seed, 0.1)
+    vel = (0.6, -0.3, 0.2)
+    dt = 0.1 * min(1.0 / d for d in dims) / ((2 * p + 1) * sum(abs(v) for v in vel))
+    return dict(NeX=dims[0], NeY=dims[1], NeZ=dims[2], p=p, nstep=nstep, dt=dt,
+                centre=prm["centre"], sigma=0.1, velocity=vel)
+
+
+def test_result_is_the_same_alone_and_in_the_mix(ops):
+    target = req((3, 4, 2), 5, 40, 11)
+    srv = sdg.Server(ops)
+    alone, _ = None, None
+    t = srv.submit(**target, want_state=True)
+    res, alone = srv.wait(t)
+    assert res["status"] == 0
+    # the same request amid others: two before it, three arriving while it runs
+    others = [req((4, 2, 3), 3, 60, 21), req((2, 2, 2), 11, 30, 22), req((5, 3, 3), 2, 80, 23),
+              req((3, 3, 3), 7, 25, 24), req((2, 3, 4), 5, 50, 25)]
+    tickets = [srv.submit(**others[0]), srv.submit(**others[1])]
+    t2 = srv.submit(**target, want_state=True)
+    for o in others[2:]:
+        time.sleep(0.002)
+        tickets.append(srv.submit(**o))
+    res2, mixed = srv.wait(t2)
+    for tk in tickets:
+        assert srv.wait(tk)[0]["status"] == 0
+    assert res2["status"] == 0
+    assert np.array_equal(alone, mixed)
+    st = srv.stats()
+    assert st["completed"] == 7 and st["fatal_status"] == 0
+    srv.close()
+
+
+def test_served_result_matches_fp64_oracle_within_fp32_tolerance(ops):
+    r = req((3, 2, 3), 3, 20, 31)
+    srv = sdg.Server(ops)
+    _, q = srv.wait(srv.submit(**r, want_state=True))
+    srv.close()
+    p = r["p"]
+    c = Case(3, 2, 3, p, ic="blob", ops=ops[p])
+    X, Y, Z = W.node_coords(3, 2, 3, ops[p][0])
+
+    def mi(d):
+        return d - np.round(d)
+
+    cx, cy, cz = r["centre"]
+    q0 = np.exp(-(mi(X - cx) ** 2 + mi(Y - cy) ** 2 + mi(Z - cz) ** 2) / (2 * 0.1 ** 2))
+    n = c.nown
+    c.q[:n] = q0
+    c.u[:n], c.v[:n], c.w[:n] = r["velocity"]
+    for f in (c.q, c.u, c.v, c.w):
+        c.mesh.update_halo(f)
+    c.dt = r["dt"]
+    assert rel_l2(q, c.oracle_run(r["nstep"])) <= TOL_FP32
+
+
+def test_admission_waits_for_memory_and_rejects_what_never_fits(ops):
+    big = req((4, 4, 4), 7, 10, 41)
+    nbytes = 8 ** 3 * 64 * 36
+    srv = sdg.Server(ops, hbm_budget_bytes=int(nbytes * 1.5))  # one at a time
+    ts = [srv.submit(**big, want_state=True) for _ in range(3)]
+    outs = [srv.wait(t)[1] for t in ts]
+    assert all(np.array_equal(outs[0], o) for o in outs[1:])
+    huge = req((9, 9, 9), 11, 5, 42)
+    with pytest.raises(sdg.SdgError) as e:
+        srv.wait(srv.submit(**huge))
+    assert e.value.status == sdg.ERR_OUT_OF_MEMORY
+    srv.close()
+
+
+def test_wait_is_bounded(ops):
+    srv = sdg.Server(ops)
+    t = srv.submit(**req((6, 6, 6), 11, 400, 51))
+    with pytest.raises(sdg.SdgError) as e:
+        srv.wait(t, timeout_s=1e-4)
+    assert e.value.status == sdg.ERR_TIMEOUT
+    assert srv.wait(t, timeout_s=600)[0]["status"] == 0
+    srv.close()
