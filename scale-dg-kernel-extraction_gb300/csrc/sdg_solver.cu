@@ -37,14 +37,6 @@ __global__ void f64_to_f32_kernel(float* out, const double* in, long long n) {
     out[i] = (float)in[i];
 }
 
-__global__ void f64_to_df_kernel(float2* out, const double* in, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const dfl d = df_from_double(in[i]);
-    out[i] = make_float2(d.hi, d.lo);
-  }
-}
-
 unsigned grid_for(long long n) {
   long long nb = (n + 255) / 256;
   if (nb > 152LL * 64) nb = 152LL * 64;
@@ -90,12 +82,9 @@ int one_stage(sdg_solver* s, int stage, double dt, const double* qin,
 // Uploads one velocity component (device source) in the compute type.
 int put_velocity(sdg_solver* s, void* dst, const double* src_dev) {
   const long long n = s->ndof;
-  if (s->prec == SDG_PREC_FP64) {
+  if (s->prec != SDG_PREC_FP32) {
     SDG_CUDA_TRY(cudaMemcpyAsync(dst, src_dev, 8 * (size_t)n, cudaMemcpyDeviceToDevice,
                                  s->stream));
-  } else if (s->prec == SDG_PREC_FP64_EMU) {
-    f64_to_df_kernel<<<grid_for(n), 256, 0, s->stream>>>(static_cast<float2*>(dst), src_dev, n);
-    SDG_CUDA_TRY(cudaGetLastError());
   } else {
     f64_to_f32_kernel<<<grid_for(n), 256, 0, s->stream>>>(static_cast<float*>(dst),
                                                          src_dev, n);
@@ -107,9 +96,9 @@ int put_velocity(sdg_solver* s, void* dst, const double* src_dev) {
 // Operator tables in the layout and arithmetic each kernel family reads:
 //   FP64: D1D(Nq,Nq) and Lift_mat(Nq,Nq,Nq,6) as given;
 //   FP32: the same rounded to float;
-//   FP64_EMU: double-float tables with the geometric factors folded in:
-//     D: [6][Nq*Nq] floats = hi/lo planes of Es_x*D1D, Es_y*D1D, Es_z*D1D;
-//     Lift: [2][6*Np] floats = hi then lo plane of Lift_mat(n,f)*0.5*Fscale(f).
+//   FP64_EMU: double-float (hi, lo) pairs with the geometric factors folded
+//     in: D [3][Nq*Nq] = Es_d*D1D, R [3][Nq] = Es_d * (row sums of D1D, from
+//     the FP64 values), Lift [6*Np] = Lift_mat(n,f)*0.5*Fscale(f).
 void operator_tables(int prec, int Nq, const Box& box, const double* D1D,
                      const double* Lift_mat, std::vector<unsigned char>& dtab,
                      std::vector<unsigned char>& ltab) {
@@ -127,22 +116,32 @@ void operator_tables(int prec, int Nq, const Box& box, const double* D1D,
     for (size_t i = 0; i < nD; i++) d[i] = (float)D1D[i];
     for (size_t i = 0; i < nL; i++) l[i] = (float)Lift_mat[i];
   } else {
-    dtab.resize(4 * 6 * nD);
-    ltab.resize(4 * 2 * nL);
+    // interleaved double-float pairs: D [3][Nq*Nq], R [3][Nq], Lift [6*Np]
+    dtab.resize(8 * (3 * nD + 3 * (size_t)Nq));
+    ltab.resize(8 * nL);
     float* d = reinterpret_cast<float*>(dtab.data());
     float* l = reinterpret_cast<float*>(ltab.data());
-    for (int ax = 0; ax < 3; ax++)
+    for (int ax = 0; ax < 3; ax++) {
       for (size_t i = 0; i < nD; i++) {
         const dfl v = df_from_double(box.Es[ax] * D1D[i]);
-        d[(2 * ax) * nD + i] = v.hi;
-        d[(2 * ax + 1) * nD + i] = v.lo;
+        d[2 * (ax * nD + i)] = v.hi;
+        d[2 * (ax * nD + i) + 1] = v.lo;
       }
+      // true row sums of the FP64 operator (about 1e-16 |D|), in long double
+      for (int i = 0; i < Nq; i++) {
+        long double rs = 0.0L;
+        for (int c = 0; c < Nq; c++) rs += (long double)D1D[i + (size_t)c * Nq];
+        const dfl v = df_from_double((double)((long double)box.Es[ax] * rs));
+        d[2 * (3 * nD + ax * Nq + i)] = v.hi;
+        d[2 * (3 * nD + ax * Nq + i) + 1] = v.lo;
+      }
+    }
     const int face_axis[6] = {1, 0, 1, 0, 2, 2};  // -y,+x,+y,-x,-z,+z
     for (int f = 0; f < 6; f++)
       for (size_t n = 0; n < Np; n++) {
         const dfl v = df_from_double(Lift_mat[n + f * Np] * (0.5 * box.Fs[face_axis[f]]));
-        l[n + f * Np] = v.hi;
-        l[nL + n + f * Np] = v.lo;
+        l[2 * (n + f * Np)] = v.hi;
+        l[2 * (n + f * Np) + 1] = v.lo;
       }
   }
 }
@@ -181,7 +180,7 @@ int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
   s->box = make_box(NeX, NeY, NeZ, Lx, Ly, Lz);
   s->ndof = (long long)s->Np * s->box.Ne;
   s->stream = as_stream(stream);
-  // velocity element size: FP64, FP32, or a double-float pair
+  // velocity element size: FP64 (FP64 and emulated forms) or FP32
   const size_t es = (precision == SDG_PREC_FP32) ? 4 : 8;
   const size_t nD = (size_t)s->Nq * s->Nq, nL = 6 * (size_t)s->Np;
   // operator tables as the kernels read them (see operator_tables below)
@@ -288,7 +287,7 @@ int sdg_solver_upload(sdg_solver* s, const double* q, const double* u,
   if (!s || !q || !u || !v || !w) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
   const size_t bytes = 8 * (size_t)s->ndof;
   SDG_CUDA_TRY(cudaMemcpyAsync(s->q[s->cur], q, bytes, cudaMemcpyHostToDevice, s->stream));
-  if (s->prec == SDG_PREC_FP64) {  // FP64 velocity is copied as is
+  if (s->prec != SDG_PREC_FP32) {  // FP64 velocity is copied as is
     SDG_CUDA_TRY(cudaMemcpyAsync(s->u, u, bytes, cudaMemcpyHostToDevice, s->stream));
     SDG_CUDA_TRY(cudaMemcpyAsync(s->v, v, bytes, cudaMemcpyHostToDevice, s->stream));
     SDG_CUDA_TRY(cudaMemcpyAsync(s->w, w, bytes, cudaMemcpyHostToDevice, s->stream));

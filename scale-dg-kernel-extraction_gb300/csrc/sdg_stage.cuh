@@ -24,6 +24,7 @@
 
 #include <cuda_runtime.h>
 
+#include "sdg_df.cuh"
 #include "sdg_internal.h"
 
 namespace sdg {
@@ -126,7 +127,12 @@ __device__ __forceinline__ long long neighbor(const Box& b, long long e, int f) 
   return (long long)ex + (long long)NeX * (ey + (long long)NeY * ez);
 }
 
+// Conversions into the compute type.  FP64 -> FP32 goes through the bit
+// pattern (df_split's high part: 24 significant bits, round half up on the
+// magnitude, |x| < 2^-126 flushed to zero) because the F2F conversion runs on
+// GB300's FP64 pipe at 1/64 of the FP32 rate.
 template <typename T> __device__ __forceinline__ T to_ct(double x) { return (T)x; }
+template <> __device__ __forceinline__ float to_ct<float>(double x) { return df_split(x).hi; }
 template <typename T> __device__ __forceinline__ T to_ct(float x) { return (T)x; }
 
 
@@ -222,13 +228,27 @@ __device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, in
     const CT lf = lift_node<P>(L + n, sf + le * NFT, i, j, k);
     const CT dq = -(((Ex * dx + Ey * dy) + Ez * dz) + lf);
     const long long g = g0 + t;
-    if (a.tend_only) {
-      a.q_out[g] = (double)dq;
+    if constexpr (sizeof(CT) == 8) {
+      if (a.tend_only) {
+        a.q_out[g] = (double)dq;
+      } else {
+        const double qv = qin[g];
+        double r = a.b * (qv + a.dt * (double)dq);
+        if (a.a != 0.0) r = a.a * a.q0[g] + r;
+        a.q_out[g] = r;
+      }
     } else {
-      const double qv = qin[g];
-      double r = a.b * (qv + a.dt * (double)dq);
-      if (a.a != 0.0) r = a.a * a.q0[g] + r;
-      a.q_out[g] = r;
+      // FP32 form: the increment (b*dt)*dqdt is an FP32 product widened by
+      // bits; the state combination a*q0 + b*q + increment stays FP64
+      if (a.tend_only) {
+        a.q_out[g] = f32_to_f64_bits(dq);
+      } else {
+        const double inc = f32_to_f64_bits(a.cdt_hi * dq);
+        const double qv = qin[g];
+        double r = (a.b == 1.0) ? qv + inc : fma(a.b, qv, inc);
+        if (a.a != 0.0) r = fma(a.a, a.q0[g], r);
+        a.q_out[g] = r;
+      }
     }
   }
 }

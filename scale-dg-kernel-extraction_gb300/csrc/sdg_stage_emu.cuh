@@ -1,27 +1,37 @@
 // Fused RK-stage kernel with emulated FP64 arithmetic (SDG_PREC_FP64_EMU).
 //
-// Same phases and data flow as stage_kernel (sdg_stage.cuh), but the flux,
-// divergence and lift arithmetic runs in double-float (sdg_df.cuh) on the
-// FP32 pipes.  The state stays FP64 in HBM, the RK combine runs in FP64, and
-// the result matches the FP64 oracle to <= 1e-12 relative L2 per tendency
-// (tested for p = 1..15).
+// GB300 runs FP64 at 1/64 of the FP32 rate, so this kernel keeps on the FP64
+// pipe only the operations whose rounding decides the accuracy, and runs the
+// long sums in double-float (sdg_df.cuh) on the FP32 pipes:
 //
-// Algebraic folds (exact in real arithmetic, so only rounding changes):
-//   - Escale_d is folded into the differentiation tables: Dd = Es_d * D1D;
-//   - 0.5*Fscale of each face is folded into the lift table:
-//     L'(n,f) = Lift_mat(n,f) * 0.5 * Fscale(f);
-//   - the whole tendency of a node is one compensated dot product
-//       dqdt = -( sum_l Dx(i,l) Fx(l,j,k) + sum_l Dy(j,l) Fy(i,l,k)
-//               + sum_l Dz(k,l) Fz(i,j,l) + sum_f L'(n,f) g_f )
-//     where g_f = qP velP - qM velM - alpha (qP - qM) is the unscaled upwind
-//     flux (mod_advect3d_eq.f90:134-139) and F_d = q u_d (:181-183);
-//   - the RK combine a*q0 + b*(q + dt*dqdt) (main.f90:70-71) is evaluated as
-//     a*q0 + b*q + (b*dt)*dqdt with the last product in double-float.
-// FP64 values enter through df_split and leave through f32_to_f64_bits, both
-// integer/FP32 code, so the FP64 pipe (1/64 of the FP32 rate on GB300) only
-// runs the two or three additions of the RK combine per node.
-// The GENERAL / OPT1 summation orders have no meaning here: the compensated
-// sum is more accurate than either.
+//   FP64:   F_d = q * u_d (the reference's flux_x = q*u, rounded the same
+//           way), the per-line differences G_d = F_d - F_d(line node 0), the
+//           face jumps q+ - q- and V+ - V-, and the RK combine;
+//   double-float: everything else.
+//
+// Why differences: sum_l D(i,l) F(l) cancels heavily (D annihilates
+// constants), so an error of 2^-48 |F| per operand would be amplified by
+// sum|D| / |derivative| (about 200 at p=7 on 32^3).  With
+//   sum_l D(i,l) F(l) = sum_l D(i,l) G(l) + F(0) * R(i),  R(i) = sum_l D(i,l)
+// (R taken from the FP64 operator, not from its double-float table), the
+// double-float rounding only touches the small differences G, and the result
+// agrees with the FP64 oracle to about 1e-14.  The upwind flux is rewritten
+// the same way: qP VP - qM VM - alpha (qP - qM) = qP (VP - VM) + (qP - qM)(VM
+// - alpha), with the jumps formed in FP64 (mod_advect3d_eq.f90:124-139).
+//
+// Layout and schedule: one block owns EPB elements and one thread one
+// "line" (Nq nodes along an axis) per phase, so each loaded value feeds Nq
+// outputs.  Per element, shared memory holds three planes of Np slots (one
+// per axis, each laid out line-major for its axis with a pad of one slot per
+// line against bank conflicts): FP64 F first, then the double-float G in
+// place, then the running compensated sums (in the x plane).  Phases:
+//   0  F = q u_d  -> planes (FP64)
+//   1  line bases F(node 0) (FP64) and the face fluxes g (double-float)
+//   2  G = F - F(node 0) in place, split to double-float
+//   3x per x-line: sum over l for every i, plus F0 * R_x  -> running sums
+//   3y per y-line: add the y sums
+//   3z per z-line: add the z sums and the lift, finish the sum, RK combine.
+// Escale is folded into the D tables and R; 0.5*Fscale into the lift table.
 #pragma once
 
 #include "sdg_df.cuh"
@@ -31,150 +41,224 @@ namespace sdg {
 
 template <int P>
 struct EmuCfg {
-  static constexpr int EPB = StageCfg<P, float>::EPB;
-  static constexpr int THREADS = StageCfg<P, float>::THREADS;
+  static constexpr int NQ2 = (P + 1) * (P + 1);
+  static constexpr int EPB = (256 / NQ2) > 0 ? (256 / NQ2) : 1;
+  static constexpr int LINES = EPB * NQ2;
+  static constexpr int THREADS = ((LINES + 31) / 32) * 32;
+  static constexpr int PADL = P + 2;            // slots per line (Nq + 1)
+  static constexpr int PLANE = PADL * NQ2;      // slots per plane
 };
 
-// floats of shared memory: D tables (3 axes x hi/lo), then per element
-// q (2 NP), u, v, w (6 NP), face fluxes g (2 NFT)
+// Device table layout (float2 = hi, lo):
+//   D:    [3][Nq*Nq]  Es_d * D1D(i,l) at l*Nq + i, axes x, y, z
+//   R:    [3][Nq]     Es_d * sum_l D1D(i,l) from the FP64 operator
+//   Lift: [6*Np]      Lift_mat(n,f) * 0.5 * Fscale(f) at n + f*Np
 template <int P>
 constexpr size_t emu_smem_bytes() {
-  using O = Ord<P>;
-  return sizeof(float) * (size_t)(6 * O::NQ2 + EmuCfg<P>::EPB * (8 * O::NP + 2 * O::NFT));
+  using C = EmuCfg<P>;
+  constexpr int NQ = P + 1, NQ2 = NQ * NQ, NFT = 6 * NQ2;
+  // tables + per element: 3 planes, 3*NQ2 line bases (FP64), NFT fluxes
+  return 8 * (size_t)(3 * NQ2 + 3 * NQ) +
+         (size_t)C::EPB * (8 * 3 * C::PLANE + 8 * 3 * NQ2 + 8 * NFT);
 }
 
 template <int P>
 __global__ void __launch_bounds__(EmuCfg<P>::THREADS) stage_emu_kernel(const StageArgs a) {
   using O = Ord<P>;
+  using C = EmuCfg<P>;
   constexpr int NQ = O::NQ, NQ2 = O::NQ2, NP = O::NP, NFP = O::NFP, NFT = O::NFT,
-                EPB = EmuCfg<P>::EPB, T = EmuCfg<P>::THREADS;
+                EPB = C::EPB, PADL = C::PADL, PLANE = C::PLANE;
+  const int T = blockDim.x;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* sD = reinterpret_cast<float*>(smem_raw);  // [6][NQ2]: Dx hi, lo, Dy hi, lo, Dz hi, lo
-  float* sqh = sD + 6 * NQ2;
-  float* sql = sqh + EPB * NP;
-  float* svh = sql + EPB * NP;  // [3][EPB*NP] hi planes of u, v, w
-  float* svl = svh + 3 * EPB * NP;
-  float* sgh = svl + 3 * EPB * NP;
-  float* sgl = sgh + EPB * NFT;
+  float2* sD = reinterpret_cast<float2*>(smem_raw);     // [3][NQ2]
+  float2* sR = sD + 3 * NQ2;                            // [3][NQ]
+  double* sPl = reinterpret_cast<double*>(sR + 3 * NQ); // [EPB][3][PLANE] (FP64 or float2)
+  double* sF0 = sPl + EPB * 3 * PLANE;                  // [EPB][3][NQ2] line bases
+  float2* sg = reinterpret_cast<float2*>(sF0 + EPB * 3 * NQ2);  // [EPB][NFT]
 
   const long long eb = a.elem_begin + (long long)blockIdx.x * EPB;
   const long long eend = a.elem_begin + a.elem_count;
   const int nloc = (int)((eend - eb) < EPB ? (eend - eb) : EPB);
   if (nloc <= 0) return;
   const double* __restrict__ qin = a.q_in;
-  const float2* __restrict__ gu = static_cast<const float2*>(a.u);
-  const float2* __restrict__ gv = static_cast<const float2*>(a.v);
-  const float2* __restrict__ gw = static_cast<const float2*>(a.w);
+  const double* __restrict__ gu = static_cast<const double*>(a.u);
+  const double* __restrict__ gv = static_cast<const double*>(a.v);
+  const double* __restrict__ gw = static_cast<const double*>(a.w);
   const long long g0 = eb * NP;
-  constexpr int SV = EPB * NP;  // stride between the u, v, w planes
 
-  // phase 0: stage state (split to double-float) and velocity
-  for (int t = threadIdx.x; t < 6 * NQ2; t += T) sD[t] = static_cast<const float*>(a.D)[t];
+  // slot of node (i,j,k) in the plane of axis d (line-major for that axis)
+  auto slot = [](int d, int i, int j, int k) -> int {
+    return (d == 0) ? i + PADL * (j + NQ * k) : (d == 1) ? j + PADL * (i + NQ * k)
+                                                         : k + PADL * (i + NQ * j);
+  };
+
+  // phase 0: tables, F = q u_d in FP64 into the planes
+  {
+    const float2* tab = static_cast<const float2*>(a.D);
+    for (int t = threadIdx.x; t < 3 * NQ2 + 3 * NQ; t += T) sD[t] = tab[t];
+  }
   for (int t = threadIdx.x; t < nloc * NP; t += T) {
-    const dfl q = df_split(qin[g0 + t]);
-    sqh[t] = q.hi;
-    sql[t] = q.lo;
-    const float2 uu = gu[g0 + t], vv = gv[g0 + t], ww = gw[g0 + t];
-    svh[t] = uu.x;
-    svl[t] = uu.y;
-    svh[SV + t] = vv.x;
-    svl[SV + t] = vv.y;
-    svh[2 * SV + t] = ww.x;
-    svl[2 * SV + t] = ww.y;
+    const int le = t / NP;
+    const int n = t - le * NP;
+    const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
+    const double qq = qin[g0 + t];
+    double* pl = sPl + le * 3 * PLANE;
+    pl[0 * PLANE + slot(0, i, j, k)] = qq * gu[g0 + t];
+    pl[1 * PLANE + slot(1, i, j, k)] = qq * gv[g0 + t];
+    pl[2 * PLANE + slot(2, i, j, k)] = qq * gw[g0 + t];
   }
   __syncthreads();
 
-  // phase 1: unscaled upwind flux g on every face node
+  // phase 1a: line bases F(node 0) of every line, kept in FP64
+  for (int r = threadIdx.x; r < nloc * 3 * NQ2; r += T) {
+    const int le = r / (3 * NQ2);
+    const int rr = r - le * 3 * NQ2;
+    const int d = rr / NQ2, line = rr - d * NQ2;
+    sF0[r] = sPl[le * 3 * PLANE + d * PLANE + PADL * line];
+  }
+  // phase 1b: upwind face fluxes g = qP (VP - VM) + (qP - qM)(VM - alpha)
   for (int t = threadIdx.x; t < nloc * NFT; t += T) {
     const int le = t / NFT;
     const int r = t - le * NFT;
     const int f = r / NFP;
     const int fp = r - f * NFP;
-    int nM, nP, axis, sg;
-    face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sg);
+    int nM, nP, axis, sgi;
+    face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sgi);
     const long long eP = neighbor(a.box, eb + le, f);
-    const long long gP = eP * NP + nP;
-    const int iM = le * NP + nM;
-    const float sgn = (float)sg;
-    const dfl qM = df_make(sqh[iM], sql[iM]);
-    const dfl velM = df_make(sgn * svh[axis * SV + iM], sgn * svl[axis * SV + iM]);
-    const dfl qP = df_split(qin[gP]);
-    const float2 vp = ((axis == 0) ? gu : (axis == 1) ? gv : gw)[gP];
-    const dfl velP = df_make(sgn * vp.x, sgn * vp.y);
-    const dfl alpha = df_scale2(df_abs(df_add(velP, velM)), 0.5f);
-    const dfl jump = df_sub(qP, qM);
+    const long long gM = (eb + le) * NP + nM, gP = eP * NP + nP;
+    const double* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
+    const double sgn = (double)sgi;
+    const double qM = qin[gM], qP = qin[gP];
+    const double VM = sgn * gvel[gM], VP = sgn * gvel[gP];
+    const double jq = qP - qM, jV = VP - VM;  // FP64 jumps
+    const dfl dVM = df_split(VM);
+    const dfl alpha = df_scale2(df_abs(df_add(df_split(VP), dVM)), 0.5f);
     dacc A = dacc_zero();
-    dacc_fma(A, qP, velP);
-    dacc_fma(A, df_neg(qM), velM);
-    dacc_fma(A, df_neg(alpha), jump);
-    const dfl gflux = dacc_result(A);
-    sgh[le * NFT + r] = gflux.hi;
-    sgl[le * NFT + r] = gflux.lo;
+    dacc_fma(A, df_split(qP), df_split(jV));
+    dacc_fma(A, df_split(jq), df_sub(dVM, alpha));
+    const dfl gf = dacc_result(A);
+    sg[t] = make_float2(gf.hi, gf.lo);
   }
   __syncthreads();
 
-  // phase 2: F_d = q * u_d in place
-  for (int t = threadIdx.x; t < nloc * NP; t += T) {
-    const dfl q = df_make(sqh[t], sql[t]);
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      const dfl F = df_mul(q, df_make(svh[d * SV + t], svl[d * SV + t]));
-      svh[d * SV + t] = F.hi;
-      svl[d * SV + t] = F.lo;
-    }
-  }
-  __syncthreads();
-
-  // phase 3: one compensated dot product per node, then the RK combine
-  const float* __restrict__ Lh = static_cast<const float*>(a.Lift);
-  const float* __restrict__ Ll = Lh + 6 * NP;
-  const dfl c_dt = df_make(a.cdt_hi, a.cdt_lo);  // b*dt split on the host
+  // phase 2: G = F - F(node 0), split to double-float in place
   for (int t = threadIdx.x; t < nloc * NP; t += T) {
     const int le = t / NP;
     const int n = t - le * NP;
-    const int i = n % NQ;
-    const int j = (n / NQ) % NQ;
-    const int k = n / NQ2;
-    const int base = le * NP;
-    dacc A = dacc_zero();
+    const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
+    double* pl = sPl + le * 3 * PLANE;
+    const double* f0 = sF0 + le * 3 * NQ2;
+    const int lines[3] = {j + NQ * k, i + NQ * k, i + NQ * j};
 #pragma unroll
-    for (int l = 0; l < NQ; l++) {
-      const int fi = base + l + j * NQ + k * NQ2;
-      dacc_fma(A, df_make(sD[0 * NQ2 + l * NQ + i], sD[1 * NQ2 + l * NQ + i]),
-               df_make(svh[fi], svl[fi]));
+    for (int d = 0; d < 3; d++) {
+      const int s = d * PLANE + slot(d, i, j, k);
+      const dfl G = df_split(pl[s] - f0[d * NQ2 + lines[d]]);
+      reinterpret_cast<float2*>(pl)[s] = make_float2(G.hi, G.lo);
     }
+  }
+  __syncthreads();
+
+  // phase 3: one thread per line, Nq outputs per line
+  const int r = threadIdx.x;
+  const bool has_line = r < nloc * NQ2;
+  const int le = has_line ? r / NQ2 : 0;
+  const int line = r - le * NQ2;
+  const int la = line % NQ, lb = line / NQ;
+  float2* pl2 = reinterpret_cast<float2*>(sPl + le * 3 * PLANE);
+  const double* f0 = sF0 + le * 3 * NQ2;
+
+  // 3x: line (j, k) = (la, lb); running sums go to the x plane in place
+  if (has_line) {
+    float2 Gl[NQ];
 #pragma unroll
-    for (int l = 0; l < NQ; l++) {
-      const int fi = SV + base + i + l * NQ + k * NQ2;
-      dacc_fma(A, df_make(sD[2 * NQ2 + l * NQ + j], sD[3 * NQ2 + l * NQ + j]),
-               df_make(svh[fi], svl[fi]));
+    for (int l = 0; l < NQ; l++) Gl[l] = pl2[PADL * line + l];
+    const dfl base = df_split(f0[0 * NQ2 + line]);
+#pragma unroll
+    for (int i = 0; i < NQ; i++) {
+      dacc A = dacc_zero();
+#pragma unroll
+      for (int l = 0; l < NQ; l++) {
+        const float2 dd = sD[0 * NQ2 + l * NQ + i];
+        dacc_fma(A, df_make(dd.x, dd.y), df_make(Gl[l].x, Gl[l].y));
+      }
+      const float2 rr = sR[0 * NQ + i];
+      dacc_fma(A, df_make(rr.x, rr.y), base);
+      pl2[PADL * line + i] = make_float2(A.s, A.c);
     }
+  }
+  __syncthreads();
+
+  // 3y: line (i, k) = (la, lb)
+  if (has_line) {
+    const int i = la, k = lb;
+    float2 Gl[NQ];
 #pragma unroll
-    for (int l = 0; l < NQ; l++) {
-      const int fi = 2 * SV + base + i + j * NQ + l * NQ2;
-      dacc_fma(A, df_make(sD[4 * NQ2 + l * NQ + k], sD[5 * NQ2 + l * NQ + k]),
-               df_make(svh[fi], svl[fi]));
+    for (int l = 0; l < NQ; l++) Gl[l] = pl2[1 * PLANE + PADL * line + l];
+    const dfl base = df_split(f0[1 * NQ2 + line]);
+#pragma unroll
+    for (int j = 0; j < NQ; j++) {
+      const int s = i + PADL * (j + NQ * k);
+      const float2 acc = pl2[s];
+      dacc A;
+      A.s = acc.x;
+      A.c = acc.y;
+#pragma unroll
+      for (int l = 0; l < NQ; l++) {
+        const float2 dd = sD[1 * NQ2 + l * NQ + j];
+        dacc_fma(A, df_make(dd.x, dd.y), df_make(Gl[l].x, Gl[l].y));
+      }
+      const float2 rr = sR[1 * NQ + j];
+      dacc_fma(A, df_make(rr.x, rr.y), base);
+      pl2[s] = make_float2(A.s, A.c);
     }
-    const int gb = le * NFT;
-    const int fidx[6] = {i + k * NQ, NFP + j + k * NQ, 2 * NFP + i + k * NQ,
-                         3 * NFP + j + k * NQ, 4 * NFP + i + j * NQ, 5 * NFP + i + j * NQ};
+  }
+  __syncthreads();
+
+  // 3z: line (i, j) = (la, lb); lift, finish, RK combine, store
+  if (has_line) {
+    const int i = la, j = lb;
+    float2 Gl[NQ];
 #pragma unroll
-    for (int f = 0; f < 6; f++)
-      dacc_fma(A, df_make(__ldg(Lh + n + f * NP), __ldg(Ll + n + f * NP)),
-               df_make(sgh[gb + fidx[f]], sgl[gb + fidx[f]]));
-    const dfl dq = df_neg(dacc_result(A));
-    const long long g = g0 + t;
-    // FP32 -> FP64 widening by bit manipulation keeps the FP64 pipe for the
-    // additions of the RK combine only
-    if (a.tend_only) {
-      a.q_out[g] = f32_to_f64_bits(dq.hi) + f32_to_f64_bits(dq.lo);
-    } else {
-      const dfl inc = df_mul(c_dt, dq);  // (b*dt)*dqdt
-      const double ih = f32_to_f64_bits(inc.hi), il = f32_to_f64_bits(inc.lo);
-      const double qv = qin[g];
-      double r = ((a.b == 1.0) ? qv + ih : fma(a.b, qv, ih)) + il;
-      if (a.a != 0.0) r = fma(a.a, a.q0[g], r);
-      a.q_out[g] = r;
+    for (int l = 0; l < NQ; l++) Gl[l] = pl2[2 * PLANE + PADL * line + l];
+    const dfl base = df_split(f0[2 * NQ2 + line]);
+    const float2* __restrict__ Lt = static_cast<const float2*>(a.Lift);
+    const float2* gl = sg + le * NFT;
+    const dfl c_dt = df_make(a.cdt_hi, a.cdt_lo);
+#pragma unroll 1
+    for (int k = 0; k < NQ; k++) {
+      const int s = i + PADL * (j + NQ * k);
+      const float2 acc = pl2[s];
+      dacc A;
+      A.s = acc.x;
+      A.c = acc.y;
+#pragma unroll
+      for (int l = 0; l < NQ; l++) {
+        const float2 dd = sD[2 * NQ2 + l * NQ + k];
+        dacc_fma(A, df_make(dd.x, dd.y), df_make(Gl[l].x, Gl[l].y));
+      }
+      const float2 rr = sR[2 * NQ + k];
+      dacc_fma(A, df_make(rr.x, rr.y), base);
+      const int n = i + j * NQ + k * NQ2;
+      const int fidx[6] = {i + k * NQ, NFP + j + k * NQ, 2 * NFP + i + k * NQ,
+                           3 * NFP + j + k * NQ, 4 * NFP + i + j * NQ, 5 * NFP + i + j * NQ};
+#pragma unroll
+      for (int f = 0; f < 6; f++) {
+        const float2 L = __ldg(Lt + n + f * NP);
+        const float2 gg = gl[fidx[f]];
+        dacc_fma(A, df_make(L.x, L.y), df_make(gg.x, gg.y));
+      }
+      const dfl dq = df_neg(dacc_result(A));
+      const long long g = (eb + le) * NP + n;
+      if (a.tend_only) {
+        a.q_out[g] = f32_to_f64_bits(dq.hi) + f32_to_f64_bits(dq.lo);
+      } else {
+        const dfl inc = df_mul(c_dt, dq);  // (b*dt)*dqdt
+        const double ih = f32_to_f64_bits(inc.hi), il = f32_to_f64_bits(inc.lo);
+        const double qv = qin[g];
+        double rq = ((a.b == 1.0) ? qv + ih : fma(a.b, qv, ih)) + il;
+        if (a.a != 0.0) rq = fma(a.a, a.q0[g], rq);
+        a.q_out[g] = rq;
+      }
     }
   }
 }
