@@ -358,6 +358,40 @@ def bench_ensemble(sdg, args):
     }
 
 
+def bench_order_sweep(sdg, args):
+    """Orders 1..15 at about 16.8M DOF (Ne per axis = round(256/(p+1))), the
+    seeded blob workload, nstep steps: throughput of the FP64, emulated-FP64
+    and FP32 forms, and the relative L2 error and mass drift of the latter two
+    against the FP64 form (which matches the CPU oracle to 1e-12 per
+    tendency, tested)."""
+    import workloads as W
+    out = []
+    for p in range(1, 16):
+        ne = int(round(256.0 / (p + 1)))
+        x, D, Dt, L = sdg.operator_generate(p)
+        q, u, v, w = W.blob(ne, ne, ne, x, args.seed + p)
+        dt = W.cfl_dt(ne, ne, ne, p, u, v, w)
+        ndof = q.size
+        m0 = W.mass(q, x, ne, ne, ne)
+        row = {"p": p, "Ne": ne, "dof": ndof, "nstep": args.sweep_steps}
+        res = {}
+        for name, prec in (("fp64", sdg.PREC_FP64), ("fp64emu", sdg.PREC_FP64_EMU),
+                           ("fp32", sdg.PREC_FP32)):
+            s = sdg.Solver(ne, ne, ne, p, D, L, precision=prec)
+            s.upload(q, u, v, w)
+            ms = s.step_timed(dt, args.sweep_steps)
+            res[name] = s.download()
+            s.close()
+            row[f"{name}_gdof_updates_per_s"] = ndof * 3 * args.sweep_steps / (ms / 1e3) / 1e9
+            row[f"{name}_mass_drift"] = abs(W.mass(res[name], x, ne, ne, ne) - m0) / abs(m0)
+        ref = res["fp64"]
+        for name in ("fp64emu", "fp32"):
+            row[f"{name}_rel_l2_vs_fp64"] = float(np.linalg.norm(res[name] - ref) /
+                                                  np.linalg.norm(ref))
+        out.append(row)
+    return out
+
+
 def bench_serving(sdg, args):
     """Poisson arrivals of solves (Ne per axis U{4..32}, p U{2..11}, nstep
     U{10..500}, Gaussian tracer in a constant velocity, FP32 compute / FP64
@@ -551,6 +585,8 @@ def run_ours(args, ws, rank, local):
         line["ensemble"] = bench_ensemble(sdg, args)
     if ws == 1 and not args.no_serving:
         line["serving"] = bench_serving(sdg, args)
+    if ws == 1 and not args.no_sweep:
+        line["order_sweep"] = bench_order_sweep(sdg, args)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -574,6 +610,8 @@ def main() -> int:
     ap.add_argument("--no-emu", action="store_true",
                     help="skip the emulated-FP64 measurement beside the FP64 headline")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--sweep-steps", type=int, default=100)
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--ens-n", type=int, default=256)
     ap.add_argument("--ens-steps", type=int, default=100)

@@ -109,13 +109,17 @@ __device__ __forceinline__ void face_nodes(int f, int ta, int tb, int& nM,
 }
 
 // Neighbour across face f with periodic wrap (eval_neighbor_element,
-// mod_mesh.f90:407-483); element index e = ex + ey*NeX + ez*NeX*NeY.
-__device__ __forceinline__ long long neighbor(const Box& b, long long e, int f) {
+// mod_mesh.f90:407-483); element index e = ex + ey*NeX + ez*NeX*NeY.  The
+// element count is below 2^31 (checked at creation), so the index arithmetic
+// is 32-bit: 64-bit division is a long software sequence on the GPU.
+__device__ __forceinline__ long long neighbor(const Box& b, long long e64, int f) {
   const int NeX = b.NeX, NeY = b.NeY, NeZ = b.NeZ;
-  int ex = (int)(e % NeX);
-  long long r = e / NeX;
-  int ey = (int)(r % NeY);
-  int ez = (int)(r / NeY);
+  const unsigned e = (unsigned)e64;
+  const unsigned rxy = e / (unsigned)NeX;
+  int ex = (int)(e - rxy * (unsigned)NeX);
+  const unsigned rz = rxy / (unsigned)NeY;
+  int ey = (int)(rxy - rz * (unsigned)NeY);
+  int ez = (int)rz;
   switch (f) {
     case 0: ey = (ey == 0) ? NeY - 1 : ey - 1; break;
     case 1: ex = (ex == NeX - 1) ? 0 : ex + 1; break;
@@ -124,7 +128,7 @@ __device__ __forceinline__ long long neighbor(const Box& b, long long e, int f) 
     case 4: ez = (ez == 0) ? NeZ - 1 : ez - 1; break;
     default: ez = (ez == NeZ - 1) ? 0 : ez + 1; break;
   }
-  return (long long)ex + (long long)NeX * (ey + (long long)NeY * ez);
+  return (long long)((unsigned)ex + (unsigned)NeX * ((unsigned)ey + (unsigned)NeY * (unsigned)ez));
 }
 
 // Conversions into the compute type.  FP64 -> FP32 goes through the bit
@@ -176,7 +180,10 @@ __device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, in
   }
   __syncthreads();
 
-  // phase 1: element-boundary flux (mod_advect3d_eq.f90:116-140)
+  // phase 1: element-boundary flux (mod_advect3d_eq.f90:116-140); 0.5*Fscale
+  // is exact in either type and converted once per thread, not per node
+  const CT hfx = (CT)(0.5 * a.box.Fs[0]), hfy = (CT)(0.5 * a.box.Fs[1]),
+           hfz = (CT)(0.5 * a.box.Fs[2]);
   for (int t = threadIdx.x; t < nloc * NFT; t += T) {
     const int le = t / NFT;
     const int r = t - le * NFT;
@@ -195,8 +202,8 @@ __device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, in
     const CT qP = to_ct<CT>(qin[gP]);
     const CT velP = sgn * to_ct<CT>(gvel[gP]);
     const CT alpha = CT(0.5) * fabs(velP + velM);
-    const CT fs = (CT)a.box.Fs[axis];
-    sf[le * NFT + r] = (CT(0.5) * fs) * ((qP * velP - qM * velM) - alpha * (qP - qM));
+    const CT hfs = (axis == 0) ? hfx : (axis == 1) ? hfy : hfz;
+    sf[le * NFT + r] = hfs * ((qP * velP - qM * velM) - alpha * (qP - qM));
   }
   __syncthreads();
 

@@ -127,9 +127,10 @@ __global__ void __launch_bounds__(EmuCfg<P>::THREADS) stage_emu_kernel(const Sta
     const long long eP = neighbor(a.box, eb + le, f);
     const long long gM = (eb + le) * NP + nM, gP = eP * NP + nP;
     const double* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
-    const double sgn = (double)sgi;
     const double qM = qin[gM], qP = qin[gP];
-    const double VM = sgn * gvel[gM], VP = sgn * gvel[gP];
+    // normal velocities +-u_axis: a sign flip, not an FP64 multiply
+    const double VM = (sgi > 0) ? gvel[gM] : -gvel[gM];
+    const double VP = (sgi > 0) ? gvel[gP] : -gvel[gP];
     const double jq = qP - qM, jV = VP - VM;  // FP64 jumps
     const dfl dVM = df_split(VM);
     const dfl alpha = df_scale2(df_abs(df_add(df_split(VP), dVM)), 0.5f);

@@ -4,7 +4,6 @@
 
 #include "sdg_stage.cuh"
 #include "sdg_stage_emu.cuh"
-#include "sdg_stage_f32.cuh"
 
 namespace sdg {
 
@@ -17,8 +16,8 @@ int launch_stage_order(int prec, int opt, const StageArgs& a, cudaStream_t st) {
     if (split) return launch_stage_impl<P, double, double, kCanSplit>(a, st);
     return launch_stage_impl<P, double, double, false>(a, st);
   }
-  if (split) return launch_stage_f32_impl<P, kCanSplit>(a, st);
-  return launch_stage_f32_impl<P, false>(a, st);
+  if (split) return launch_stage_impl<P, float, float, kCanSplit>(a, st);
+  return launch_stage_impl<P, float, float, false>(a, st);
 }
 
 }  // namespace sdg
