@@ -27,6 +27,7 @@ struct BatchInst {
   const float* Lift;   // FP32 Lift_mat of this order
   Box box;
   double dt;
+  float cdt[3];        // FP32 b_s*dt of the three stages, made on the host
   int p;
   int cur;             // buffer holding the current state
   int active;          // 0: skipped by the stage kernel and by the advance
@@ -37,6 +38,12 @@ struct BatchItem {
   int e_begin;
   int e_count;
 };
+
+// FP32 increment factors b_s*dt of the three SSP-RK3 stages (mod_common.f90:30).
+inline void batch_stage_factors(BatchInst& I) {
+  const double b[3] = {1.0, 0.25, 2.0 / 3.0};
+  for (int s = 0; s < 3; s++) I.cdt[s] = (float)(b[s] * I.dt);
+}
 
 // Launches one stage over `n_items` items; counter must be zero on entry.
 int batch_stage_launch(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,

@@ -44,8 +44,10 @@ __global__ void __launch_bounds__(kBatchThreadsMax)
       a.a = c_rk_a[stage];
       a.b = c_rk_b[stage];
       a.dt = I.dt;
-      a.cdt_hi = (float)(a.b * I.dt);  // FP32 increment factor of the FP32 form
+      a.cdt_hi = I.cdt[stage];  // FP32 increment factor of the FP32 form
       a.cdt_lo = 0.0f;
+      a.b_is_one = (stage == 0);
+      a.a_nonzero = (stage != 0);
       a.tend_only = 0;
       switch (I.p) {
         case 1: run_order<1>(a, w, smem); break;

@@ -231,6 +231,7 @@ int sdg_ensemble_create(sdg_ensemble** out, int n, const int* dims, const int* o
     I.D = e->d_ops[p][0];
     I.Lift = e->d_ops[p][1];
     I.dt = dt[i];
+    batch_stage_factors(I);
     I.p = p;
     I.cur = 0;
     I.active = 1;

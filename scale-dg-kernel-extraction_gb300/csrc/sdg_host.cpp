@@ -59,7 +59,11 @@ Box make_box(int NeX, int NeY, int NeZ, double Lx, double Ly, double Lz) {
   b.Es[0] = 2.0 / dx;
   b.Es[1] = 2.0 / dy;
   b.Es[2] = 2.0 / dz;
-  for (int d = 0; d < 3; d++) b.Fs[d] = b.Es[d];
+  for (int d = 0; d < 3; d++) {
+    b.Fs[d] = b.Es[d];
+    b.Esf[d] = (float)b.Es[d];
+    b.hFsf[d] = (float)(0.5 * b.Fs[d]);
+  }
   return b;
 }
 

@@ -42,6 +42,10 @@ struct Box {
   long long Ne;
   double Es[3];  // Escale(:,:,d) = 2/dx_d  (mod_mesh.f90:147-149)
   double Fs[3];  // Fscale of the faces normal to axis d (mod_mesh.f90:366-394)
+  // FP32 copies made on the host (Es, and 0.5*Fs as the flux uses it): a
+  // conversion in the kernel would run on GB300's 1/64-rate FP64 pipe
+  float Esf[3];
+  float hFsf[3];
 };
 Box make_box(int NeX, int NeY, int NeZ, double Lx, double Ly, double Lz);
 
@@ -60,6 +64,8 @@ struct StageArgs {
   long long elem_count;  // elements of this launch
   double a, b, dt;      // q_out = a*q0 + b*(q_in + dt*dqdt)
   float cdt_hi, cdt_lo; // b*dt as a double-float pair (emulated-FP64 kernel)
+  int b_is_one;         // b == 1 (stage 1): the kernels branch on integers,
+  int a_nonzero;        // since an FP64 comparison also uses the FP64 pipe
   int tend_only;        // write dqdt instead of the RK update
 };
 

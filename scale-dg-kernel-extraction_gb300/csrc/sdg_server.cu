@@ -112,6 +112,7 @@ int admit(sdg_server* s, Req* q) {
   I.D = s->d_ops[q->r.p][0];
   I.Lift = s->d_ops[q->r.p][1];
   I.dt = q->r.dt;
+  batch_stage_factors(I);
   I.p = q->r.p;
   I.cur = 0;
   I.active = 1;

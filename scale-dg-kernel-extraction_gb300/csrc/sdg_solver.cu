@@ -75,6 +75,8 @@ int one_stage(sdg_solver* s, int stage, double dt, const double* qin,
   const dfl cdt = df_from_double(a.b * dt);
   a.cdt_hi = cdt.hi;
   a.cdt_lo = cdt.lo;
+  a.b_is_one = (a.b == 1.0) ? 1 : 0;
+  a.a_nonzero = (a.a != 0.0) ? 1 : 0;
   a.tend_only = tend_only ? 1 : 0;
   return launch_stage(s->p, s->prec, s->opt, a, s->stream);
 }

@@ -6,14 +6,13 @@
 // and cal_dqdt :146-201 with the DG operators of mod_dg_optr_kernel.f90) and
 // the RK combine of main.f90:68-73.  A block owns EPB consecutive elements:
 //
-//   phase 0  stage q,u,v,w of its elements (contiguous, coalesced) and D1D
-//            in shared memory;
+//   phase 0  D1D and the 6 neighbour elements of each element (periodic
+//            wrap, computed once per element), and the block's nodes staged
+//            in shared memory as q and F_d = q*u_d (coalesced loads);
 //   phase 1  upwind flux on all 6*Nfp face nodes of each element: the minus
-//            side comes from shared memory, the plus side is gathered from
-//            the neighbour element's opposite face (computed from the
-//            element index with periodic wrap, which is what VMapP plus the
-//            halo buffer encode);
-//   phase 2  F_d = q*u_d in place;
+//            side's q from shared memory, its velocity and the plus side's q
+//            and velocity from global memory (the neighbour's opposite face,
+//            which is what VMapP plus the halo buffer encode);
 //   phase 3  per node: sum-factorised Dx/Dy/Dz contractions, the lift of the
 //            face fluxes, dqdt = -(Es_x Dx + Es_y Dy + Es_z Dz + Lift) and
 //            q_out = a*q0 + b*(q + dt*dqdt).
@@ -140,11 +139,13 @@ template <> __device__ __forceinline__ float to_ct<float>(double x) { return df_
 template <typename T> __device__ __forceinline__ T to_ct(float x) { return (T)x; }
 
 
-// Dynamic shared memory of one block holding `nloc` elements of order P.
+// Dynamic shared memory of one block holding `nloc` elements of order P:
+// D1D, then per element q, F_x, F_y, F_z (Np each) and the face fluxes (6 Nfp),
+// then the 6 neighbour indices of every element.
 template <int P, typename CT>
 __host__ __device__ constexpr size_t stage_block_smem(int nloc) {
   using O = Ord<P>;
-  return sizeof(CT) * (size_t)(O::NQ2 + nloc * (4 * O::NP + O::NFT));
+  return sizeof(CT) * (size_t)(O::NQ2 + nloc * (4 * O::NP + O::NFT)) + sizeof(int) * 6 * nloc;
 }
 
 // One block advances elements [eb, eb + nloc) of the box in `a` through one
@@ -159,10 +160,11 @@ __device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, in
   const int T = blockDim.x;
   CT* sD = reinterpret_cast<CT*>(smem);
   CT* sq = sD + NQ2;
-  CT* su = sq + nloc * NP;
-  CT* sv = su + nloc * NP;
-  CT* sw = sv + nloc * NP;
+  CT* su = sq + nloc * NP;  // F_x after phase 0
+  CT* sv = su + nloc * NP;  // F_y
+  CT* sw = sv + nloc * NP;  // F_z
   CT* sf = sw + nloc * NP;
+  int* snb = reinterpret_cast<int*>(sf + nloc * NFT);
 
   const double* __restrict__ qin = a.q_in;
   const VT* __restrict__ gu = static_cast<const VT*>(a.u);
@@ -170,20 +172,35 @@ __device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, in
   const VT* __restrict__ gw = static_cast<const VT*>(a.w);
   const long long g0 = eb * NP;
 
-  // phase 0: stage the block's elements
+  // phase 0: D1D, neighbour elements (once per element, not per face node),
+  // and the staged state with the volume fluxes F_d = q * u_d
+  // (mod_advect3d_eq.f90:181-183)
   for (int t = threadIdx.x; t < NQ2; t += T) sD[t] = static_cast<const CT*>(a.D)[t];
+  for (int t = threadIdx.x; t < 6 * nloc; t += T)
+    snb[t] = (int)neighbor(a.box, eb + t / 6, t % 6);
   for (int t = threadIdx.x; t < nloc * NP; t += T) {
-    sq[t] = to_ct<CT>(qin[g0 + t]);
-    su[t] = to_ct<CT>(gu[g0 + t]);
-    sv[t] = to_ct<CT>(gv[g0 + t]);
-    sw[t] = to_ct<CT>(gw[g0 + t]);
+    const CT qq = to_ct<CT>(qin[g0 + t]);
+    sq[t] = qq;
+    su[t] = qq * to_ct<CT>(gu[g0 + t]);
+    sv[t] = qq * to_ct<CT>(gv[g0 + t]);
+    sw[t] = qq * to_ct<CT>(gw[g0 + t]);
   }
   __syncthreads();
 
   // phase 1: element-boundary flux (mod_advect3d_eq.f90:116-140); 0.5*Fscale
-  // is exact in either type and converted once per thread, not per node
-  const CT hfx = (CT)(0.5 * a.box.Fs[0]), hfy = (CT)(0.5 * a.box.Fs[1]),
-           hfz = (CT)(0.5 * a.box.Fs[2]);
+  // is exact in either type and prepared on the host for FP32.  The velocity
+  // of both sides is read from global memory (the own element's values were
+  // just loaded by phase 0 and sit in L1).
+  CT hfx, hfy, hfz;
+  if constexpr (sizeof(CT) == 4) {
+    hfx = a.box.hFsf[0];
+    hfy = a.box.hFsf[1];
+    hfz = a.box.hFsf[2];
+  } else {
+    hfx = 0.5 * a.box.Fs[0];
+    hfy = 0.5 * a.box.Fs[1];
+    hfz = 0.5 * a.box.Fs[2];
+  }
   for (int t = threadIdx.x; t < nloc * NFT; t += T) {
     const int le = t / NFT;
     const int r = t - le * NFT;
@@ -191,34 +208,34 @@ __device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, in
     const int fp = r - f * NFP;
     int nM, nP, axis, sg;
     face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sg);
-    const long long eP = neighbor(a.box, eb + le, f);
-    const CT* svel = (axis == 0) ? su : (axis == 1) ? sv : sw;
+    const long long gM = g0 + (long long)le * NP + nM;
+    const long long gP = (long long)snb[6 * le + f] * NP + nP;
     const VT* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
-    const long long gP = eP * NP + nP;
-    // normal velocity u.n with an axis-aligned unit normal is +-u_axis exactly
-    const CT sgn = (CT)sg;
+    // normal velocity u.n with an axis-aligned unit normal is +-u_axis
+    // exactly; the sign is applied by negation, not by a multiply
+    const CT uM = to_ct<CT>(gvel[gM]), uP = to_ct<CT>(gvel[gP]);
+    const CT velM = (sg > 0) ? uM : -uM;
+    const CT velP = (sg > 0) ? uP : -uP;
     const CT qM = sq[le * NP + nM];
-    const CT velM = sgn * svel[le * NP + nM];
     const CT qP = to_ct<CT>(qin[gP]);
-    const CT velP = sgn * to_ct<CT>(gvel[gP]);
     const CT alpha = CT(0.5) * fabs(velP + velM);
     const CT hfs = (axis == 0) ? hfx : (axis == 1) ? hfy : hfz;
     sf[le * NFT + r] = hfs * ((qP * velP - qM * velM) - alpha * (qP - qM));
   }
   __syncthreads();
 
-  // phase 2: volume fluxes F_d = q * u_d (mod_advect3d_eq.f90:181-183)
-  for (int t = threadIdx.x; t < nloc * NP; t += T) {
-    const CT qq = sq[t];
-    su[t] = qq * su[t];
-    sv[t] = qq * sv[t];
-    sw[t] = qq * sw[t];
-  }
-  __syncthreads();
-
   // phase 3: divergence + lift + combine + RK (mod_advect3d_eq.f90:185-198,
   // main.f90:69-73)
-  const CT Ex = (CT)a.box.Es[0], Ey = (CT)a.box.Es[1], Ez = (CT)a.box.Es[2];
+  CT Ex, Ey, Ez;
+  if constexpr (sizeof(CT) == 4) {
+    Ex = a.box.Esf[0];
+    Ey = a.box.Esf[1];
+    Ez = a.box.Esf[2];
+  } else {
+    Ex = a.box.Es[0];
+    Ey = a.box.Es[1];
+    Ez = a.box.Es[2];
+  }
   const CT* __restrict__ L = static_cast<const CT*>(a.Lift);
   for (int t = threadIdx.x; t < nloc * NP; t += T) {
     const int le = t / NP;
@@ -241,7 +258,7 @@ __device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, in
       } else {
         const double qv = qin[g];
         double r = a.b * (qv + a.dt * (double)dq);
-        if (a.a != 0.0) r = a.a * a.q0[g] + r;
+        if (a.a_nonzero) r = a.a * a.q0[g] + r;
         a.q_out[g] = r;
       }
     } else {
@@ -252,8 +269,8 @@ __device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, in
       } else {
         const double inc = f32_to_f64_bits(a.cdt_hi * dq);
         const double qv = qin[g];
-        double r = (a.b == 1.0) ? qv + inc : fma(a.b, qv, inc);
-        if (a.a != 0.0) r = fma(a.a, a.q0[g], r);
+        double r = a.b_is_one ? qv + inc : fma(a.b, qv, inc);
+        if (a.a_nonzero) r = fma(a.a, a.q0[g], r);
         a.q_out[g] = r;
       }
     }

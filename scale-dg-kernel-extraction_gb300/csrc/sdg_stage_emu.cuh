@@ -4,9 +4,10 @@
 // pipe only the operations whose rounding decides the accuracy, and runs the
 // long sums in double-float (sdg_df.cuh) on the FP32 pipes:
 //
-//   FP64:   F_d = q * u_d (the reference's flux_x = q*u, rounded the same
-//           way), the per-line differences G_d = F_d - F_d(line node 0), the
-//           face jumps q+ - q- and V+ - V-, and the RK combine;
+//   FP64:   the line bases F0 = q u_d at each line's node 0 (rounded as the
+//           reference rounds flux_x = q*u), the per-line differences
+//           G_d = q u_d - F0 as one FMA (exact product minus the base, rounded
+//           once), the face jumps q+ - q- and V+ - V-, and the RK combine;
 //   double-float: everything else.
 //
 // Why differences: sum_l D(i,l) F(l) cancels heavily (D annihilates
@@ -23,11 +24,11 @@
 // "line" (Nq nodes along an axis) per phase, so each loaded value feeds Nq
 // outputs.  Per element, shared memory holds three planes of Np slots (one
 // per axis, each laid out line-major for its axis with a pad of one slot per
-// line against bank conflicts): FP64 F first, then the double-float G in
-// place, then the running compensated sums (in the x plane).  Phases:
-//   0  F = q u_d  -> planes (FP64)
-//   1  line bases F(node 0) (FP64) and the face fluxes g (double-float)
-//   2  G = F - F(node 0) in place, split to double-float
+// line against bank conflicts): the double-float differences G, then the
+// running compensated sums (in the x plane).  Phases:
+//   0  tables, neighbour elements, line bases F0 (FP64)
+//   1  face fluxes g (double-float) and G = fma(q, u_d, -F0) split to
+//      double-float into the planes
 //   3x per x-line: sum over l for every i, plus F0 * R_x  -> running sums
 //   3y per y-line: add the y sums
 //   3z per z-line: add the z sums and the lift, finish the sum, RK combine.
@@ -57,9 +58,10 @@ template <int P>
 constexpr size_t emu_smem_bytes() {
   using C = EmuCfg<P>;
   constexpr int NQ = P + 1, NQ2 = NQ * NQ, NFT = 6 * NQ2;
-  // tables + per element: 3 planes, 3*NQ2 line bases (FP64), NFT fluxes
+  // tables + per element: 3 planes, 3*NQ2 line bases (FP64), NFT fluxes,
+  // 6 neighbour indices (padded to 8 for alignment)
   return 8 * (size_t)(3 * NQ2 + 3 * NQ) +
-         (size_t)C::EPB * (8 * 3 * C::PLANE + 8 * 3 * NQ2 + 8 * NFT);
+         (size_t)C::EPB * (8 * 3 * C::PLANE + 8 * 3 * NQ2 + 8 * NFT + 4 * 8);
 }
 
 template <int P>
@@ -75,6 +77,7 @@ __global__ void __launch_bounds__(EmuCfg<P>::THREADS) stage_emu_kernel(const Sta
   double* sPl = reinterpret_cast<double*>(sR + 3 * NQ); // [EPB][3][PLANE] (FP64 or float2)
   double* sF0 = sPl + EPB * 3 * PLANE;                  // [EPB][3][NQ2] line bases
   float2* sg = reinterpret_cast<float2*>(sF0 + EPB * 3 * NQ2);  // [EPB][NFT]
+  int* snb = reinterpret_cast<int*>(sg + EPB * NFT);             // [EPB][8]
 
   const long long eb = a.elem_begin + (long long)blockIdx.x * EPB;
   const long long eend = a.elem_begin + a.elem_count;
@@ -92,31 +95,27 @@ __global__ void __launch_bounds__(EmuCfg<P>::THREADS) stage_emu_kernel(const Sta
                                                          : k + PADL * (i + NQ * j);
   };
 
-  // phase 0: tables, F = q u_d in FP64 into the planes
+  // phase 0: tables, neighbour elements, line bases F0 = q u_d at node 0
   {
     const float2* tab = static_cast<const float2*>(a.D);
     for (int t = threadIdx.x; t < 3 * NQ2 + 3 * NQ; t += T) sD[t] = tab[t];
   }
-  for (int t = threadIdx.x; t < nloc * NP; t += T) {
-    const int le = t / NP;
-    const int n = t - le * NP;
-    const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
-    const double qq = qin[g0 + t];
-    double* pl = sPl + le * 3 * PLANE;
-    pl[0 * PLANE + slot(0, i, j, k)] = qq * gu[g0 + t];
-    pl[1 * PLANE + slot(1, i, j, k)] = qq * gv[g0 + t];
-    pl[2 * PLANE + slot(2, i, j, k)] = qq * gw[g0 + t];
-  }
-  __syncthreads();
-
-  // phase 1a: line bases F(node 0) of every line, kept in FP64
+  for (int t = threadIdx.x; t < 6 * nloc; t += T)
+    snb[8 * (t / 6) + t % 6] = (int)neighbor(a.box, eb + t / 6, t % 6);
   for (int r = threadIdx.x; r < nloc * 3 * NQ2; r += T) {
     const int le = r / (3 * NQ2);
     const int rr = r - le * 3 * NQ2;
     const int d = rr / NQ2, line = rr - d * NQ2;
-    sF0[r] = sPl[le * 3 * PLANE + d * PLANE + PADL * line];
+    const int la = line % NQ, lb = line / NQ;
+    // node 0 of the line: x-line (0, j, k), y-line (i, 0, k), z-line (i, j, 0)
+    const int n0 = (d == 0) ? NQ * la + NQ2 * lb : (d == 1) ? la + NQ2 * lb : la + NQ * lb;
+    const long long g = g0 + (long long)le * NP + n0;
+    const double* gvel = (d == 0) ? gu : (d == 1) ? gv : gw;
+    sF0[r] = qin[g] * gvel[g];
   }
-  // phase 1b: upwind face fluxes g = qP (VP - VM) + (qP - qM)(VM - alpha)
+  __syncthreads();
+
+  // phase 1a: upwind face fluxes g = qP (VP - VM) + (qP - qM)(VM - alpha)
   for (int t = threadIdx.x; t < nloc * NFT; t += T) {
     const int le = t / NFT;
     const int r = t - le * NFT;
@@ -124,8 +123,8 @@ __global__ void __launch_bounds__(EmuCfg<P>::THREADS) stage_emu_kernel(const Sta
     const int fp = r - f * NFP;
     int nM, nP, axis, sgi;
     face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sgi);
-    const long long eP = neighbor(a.box, eb + le, f);
-    const long long gM = (eb + le) * NP + nM, gP = eP * NP + nP;
+    const long long gM = g0 + (long long)le * NP + nM;
+    const long long gP = (long long)snb[8 * le + f] * NP + nP;
     const double* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
     const double qM = qin[gM], qP = qin[gP];
     // normal velocities +-u_axis: a sign flip, not an FP64 multiply
@@ -140,22 +139,20 @@ __global__ void __launch_bounds__(EmuCfg<P>::THREADS) stage_emu_kernel(const Sta
     const dfl gf = dacc_result(A);
     sg[t] = make_float2(gf.hi, gf.lo);
   }
-  __syncthreads();
-
-  // phase 2: G = F - F(node 0), split to double-float in place
+  // phase 1b: G = q u_d - F0 (one FMA), split to double-float into the planes
   for (int t = threadIdx.x; t < nloc * NP; t += T) {
     const int le = t / NP;
     const int n = t - le * NP;
     const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
-    double* pl = sPl + le * 3 * PLANE;
+    float2* pl = reinterpret_cast<float2*>(sPl + le * 3 * PLANE);
     const double* f0 = sF0 + le * 3 * NQ2;
-    const int lines[3] = {j + NQ * k, i + NQ * k, i + NQ * j};
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      const int s = d * PLANE + slot(d, i, j, k);
-      const dfl G = df_split(pl[s] - f0[d * NQ2 + lines[d]]);
-      reinterpret_cast<float2*>(pl)[s] = make_float2(G.hi, G.lo);
-    }
+    const double qq = qin[g0 + t];
+    const dfl Gx = df_split(fma(qq, gu[g0 + t], -f0[0 * NQ2 + j + NQ * k]));
+    const dfl Gy = df_split(fma(qq, gv[g0 + t], -f0[1 * NQ2 + i + NQ * k]));
+    const dfl Gz = df_split(fma(qq, gw[g0 + t], -f0[2 * NQ2 + i + NQ * j]));
+    pl[0 * PLANE + slot(0, i, j, k)] = make_float2(Gx.hi, Gx.lo);
+    pl[1 * PLANE + slot(1, i, j, k)] = make_float2(Gy.hi, Gy.lo);
+    pl[2 * PLANE + slot(2, i, j, k)] = make_float2(Gz.hi, Gz.lo);
   }
   __syncthreads();
 
@@ -256,8 +253,8 @@ __global__ void __launch_bounds__(EmuCfg<P>::THREADS) stage_emu_kernel(const Sta
         const dfl inc = df_mul(c_dt, dq);  // (b*dt)*dqdt
         const double ih = f32_to_f64_bits(inc.hi), il = f32_to_f64_bits(inc.lo);
         const double qv = qin[g];
-        double rq = ((a.b == 1.0) ? qv + ih : fma(a.b, qv, ih)) + il;
-        if (a.a != 0.0) rq = fma(a.a, a.q0[g], rq);
+        double rq = (a.b_is_one ? qv + ih : fma(a.b, qv, ih)) + il;
+        if (a.a_nonzero) rq = fma(a.a, a.q0[g], rq);
         a.q_out[g] = rq;
       }
     }
