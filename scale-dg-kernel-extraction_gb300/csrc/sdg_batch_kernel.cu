@@ -1,6 +1,5 @@
 // The persistent batched stage kernel and its helpers (see sdg_batch.cuh).
 #include "sdg_batch.cuh"
-#include "sdg_stage_col.cuh"
 
 namespace sdg {
 
@@ -13,7 +12,7 @@ __constant__ double c_rk_b[3] = {1.0, 0.25, 2.0 / 3.0};
 template <int P>
 __device__ __forceinline__ void run_order(const StageArgs& a, const BatchItem& w,
                                           unsigned char* smem) {
-  stage_block_col<P, false>(a, w.e_begin, w.e_count, smem);
+  stage_block<P, float, float, false>(a, w.e_begin, w.e_count, smem);
 }
 
 __global__ void __launch_bounds__(kBatchThreadsMax)
@@ -105,7 +104,7 @@ __global__ void init_blob_kernel(double* q, float* u, float* v, float* w, const 
 
 template <int P>
 size_t smem_for(int epb) {
-  return col_block_smem<P>(epb);
+  return stage_block_smem<P, float>(epb);
 }
 
 }  // namespace

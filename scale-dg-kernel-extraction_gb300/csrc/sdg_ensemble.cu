@@ -35,10 +35,10 @@ struct sdg_ensemble {
 
 namespace {
 
-// Default elements per block: about 256 columns (one per thread) per block.
+// Default elements per block: about 512 nodes per block.
 int default_epb(int p) {
-  const int nq2 = (p + 1) * (p + 1);
-  int e = 256 / nq2;
+  const int np = (p + 1) * (p + 1) * (p + 1);
+  int e = 512 / np;
   return e < 1 ? 1 : e;
 }
 

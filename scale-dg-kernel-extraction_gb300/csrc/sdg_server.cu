@@ -327,8 +327,8 @@ int sdg_server_create(sdg_server** out, const sdg_server_config* cfg,
   s->cfg = *cfg;
   if (s->cfg.threads > 0) s->threads = s->cfg.threads;
   for (int p = 0; p <= kBatchMaxOrder; p++) {
-    const int nq2 = (p + 1) * (p + 1);
-    s->epb[p] = std::max(1, 256 / nq2);
+    const int np = (p + 1) * (p + 1) * (p + 1);
+    s->epb[p] = std::max(1, 512 / np);
     if (cfg->epb_by_order[p] > 0) s->epb[p] = cfg->epb_by_order[p];
   }
   auto bail = [&](int st) {

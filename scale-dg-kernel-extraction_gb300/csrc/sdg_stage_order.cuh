@@ -3,7 +3,6 @@
 #pragma once
 
 #include "sdg_stage.cuh"
-#include "sdg_stage_col.cuh"
 #include "sdg_stage_emu.cuh"
 
 namespace sdg {
@@ -17,8 +16,8 @@ int launch_stage_order(int prec, int opt, const StageArgs& a, cudaStream_t st) {
     if (split) return launch_stage_impl<P, double, double, kCanSplit>(a, st);
     return launch_stage_impl<P, double, double, false>(a, st);
   }
-  if (split) return launch_stage_col_impl<P, kCanSplit>(a, st);
-  return launch_stage_col_impl<P, false>(a, st);
+  if (split) return launch_stage_impl<P, float, float, kCanSplit>(a, st);
+  return launch_stage_impl<P, float, float, false>(a, st);
 }
 
 }  // namespace sdg
