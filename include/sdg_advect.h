@@ -230,6 +230,20 @@ int sdg_solver_step(sdg_solver* s, double dt, int nstep);
 int sdg_solver_step_timed(sdg_solver* s, double dt, int nstep, double* ms);
 /* Copies q (owned part, Np*Ne values) to host memory; synchronises. */
 int sdg_solver_download(sdg_solver* s, double* q);
+/* Host-to-host solves, pipelined: for each request r < count, uploads
+ * q_in[r], u[r], v[r], w[r] (host memory, Np*Ne values each), advances nstep
+ * steps of size dt from that state and downloads the result into q_out[r].
+ * Two device buffer sets and separate upload / compute / download streams let
+ * request r+1's upload and request r-1's download overlap request r's kernels
+ * (page-locked host memory is needed for the overlap).  The solver's own
+ * state is not touched; the extra buffers are allocated on first use.
+ * Synchronises before returning. */
+int sdg_solver_solve_host_pipelined(sdg_solver* s, int count,
+                                    const double* const* q_in,
+                                    const double* const* u,
+                                    const double* const* v,
+                                    const double* const* w,
+                                    double* const* q_out, double dt, int nstep);
 /* Device pointer of the current state q (Np*Ne doubles). */
 const double* sdg_solver_state_dev(const sdg_solver* s);
 /* Evaluates the tendency of the current state into dqdt (owned part,

@@ -14,6 +14,15 @@
 
 using namespace sdg;
 
+// One device copy of a solve's buffers, for the pipelined host-to-host path.
+struct IoSlot {
+  double* q[3] = {nullptr, nullptr, nullptr};
+  void* u = nullptr;
+  void* v = nullptr;
+  void* w = nullptr;
+  cudaEvent_t uploaded = nullptr, computed = nullptr, downloaded = nullptr;
+};
+
 struct sdg_solver {
   int p = 0, Nq = 0, Np = 0, opt = 0, prec = 0;
   Box box{};
@@ -27,6 +36,10 @@ struct sdg_solver {
   void* D = nullptr;
   void* Lift = nullptr;
   double* dqdt = nullptr;
+  // pipelined host-to-host solves (allocated on first use)
+  IoSlot io[2];
+  bool io_ready = false;
+  cudaStream_t h2d = nullptr, d2h = nullptr, comp = nullptr;
 };
 
 namespace {
@@ -44,6 +57,18 @@ unsigned grid_for(long long n) {
 }
 
 void release(sdg_solver* s) {
+  for (IoSlot& io : s->io) {
+    for (int i = 0; i < 3; i++) cudaFree(io.q[i]);
+    cudaFree(io.u);
+    cudaFree(io.v);
+    cudaFree(io.w);
+    if (io.uploaded) cudaEventDestroy(io.uploaded);
+    if (io.computed) cudaEventDestroy(io.computed);
+    if (io.downloaded) cudaEventDestroy(io.downloaded);
+  }
+  if (s->h2d) cudaStreamDestroy(s->h2d);
+  if (s->d2h) cudaStreamDestroy(s->d2h);
+  if (s->comp) cudaStreamDestroy(s->comp);
   for (int i = 0; i < 3; i++) cudaFree(s->q[i]);
   cudaFree(s->u);
   cudaFree(s->v);
@@ -53,17 +78,27 @@ void release(sdg_solver* s) {
   cudaFree(s->dqdt);
 }
 
+int one_stage_on(sdg_solver* s, int stage, double dt, const double* qin, const double* q0,
+                 double* qout, const void* u, const void* v, const void* w, cudaStream_t st,
+                 bool tend_only);
+
 int one_stage(sdg_solver* s, int stage, double dt, const double* qin,
               const double* q0, double* qout, bool tend_only) {
+  return one_stage_on(s, stage, dt, qin, q0, qout, s->u, s->v, s->w, s->stream, tend_only);
+}
+
+int one_stage_on(sdg_solver* s, int stage, double dt, const double* qin, const double* q0,
+                 double* qout, const void* u, const void* v, const void* w, cudaStream_t st,
+                 bool tend_only) {
   static const double rk_a[3] = {0.0, 0.75, 1.0 / 3.0};  // mod_common.f90:28-30
   static const double rk_b[3] = {1.0, 0.25, 2.0 / 3.0};
   StageArgs a{};
   a.q_in = qin;
   a.q0 = q0;
   a.q_out = qout;
-  a.u = s->u;
-  a.v = s->v;
-  a.w = s->w;
+  a.u = u;
+  a.v = v;
+  a.w = w;
   a.D = s->D;
   a.Lift = s->Lift;
   a.box = s->box;
@@ -78,7 +113,7 @@ int one_stage(sdg_solver* s, int stage, double dt, const double* qin,
   a.b_is_one = (a.b == 1.0) ? 1 : 0;
   a.a_nonzero = (a.a != 0.0) ? 1 : 0;
   a.tend_only = tend_only ? 1 : 0;
-  return launch_stage(s->p, s->prec, s->opt, a, s->stream);
+  return launch_stage(s->p, s->prec, s->opt, a, st);
 }
 
 // Uploads one velocity component (device source) in the compute type.
@@ -350,6 +385,82 @@ int sdg_solver_tendency(sdg_solver* s, double* dqdt) {
   SDG_CUDA_TRY(cudaMemcpyAsync(dqdt, s->dqdt, 8 * (size_t)s->ndof, cudaMemcpyDeviceToHost,
                                s->stream));
   SDG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return SDG_OK;
+}
+
+// Pipelined host-to-host solves: two device buffer sets, an upload stream, a
+// compute stream and a download stream, ordered by events so that request
+// r+1's upload and request r-1's download overlap request r's kernels.
+int sdg_solver_solve_host_pipelined(sdg_solver* s, int count, const double* const* q_in,
+                                    const double* const* u, const double* const* v,
+                                    const double* const* w, double* const* q_out, double dt,
+                                    int nstep) {
+  if (!s || count < 0 || nstep < 0 || (count > 0 && (!q_in || !u || !v || !w || !q_out)))
+    return fail(SDG_ERR_INVALID_ARG, "bad pipelined solve arguments");
+  if (count == 0) return SDG_OK;
+  const size_t bytes = 8 * (size_t)s->ndof;
+  const size_t es = (s->prec == SDG_PREC_FP32) ? 4 : 8;
+  if (!s->io_ready) {
+    cudaError_t e = cudaStreamCreateWithFlags(&s->h2d, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->d2h, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->comp, cudaStreamNonBlocking);
+    for (IoSlot& io : s->io) {
+      for (int i = 0; i < 3 && e == cudaSuccess; i++) e = cudaMalloc(&io.q[i], bytes);
+      if (e == cudaSuccess) e = cudaMalloc(&io.u, es * (size_t)s->ndof);
+      if (e == cudaSuccess) e = cudaMalloc(&io.v, es * (size_t)s->ndof);
+      if (e == cudaSuccess) e = cudaMalloc(&io.w, es * (size_t)s->ndof);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&io.uploaded, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&io.computed, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&io.downloaded, cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "pipelined solve setup", __FILE__, __LINE__);
+    s->io_ready = true;
+  }
+  // the pipeline's work starts after everything already queued on the solver
+  cudaEvent_t start;
+  SDG_CUDA_TRY(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+  SDG_CUDA_TRY(cudaEventRecord(start, s->stream));
+  SDG_CUDA_TRY(cudaStreamWaitEvent(s->h2d, start, 0));
+  cudaEventDestroy(start);
+  for (int r = 0; r < count; r++) {
+    IoSlot& io = s->io[r % 2];
+    if (r >= 2) {
+      // the slot's previous request must have finished reading and downloading
+      SDG_CUDA_TRY(cudaStreamWaitEvent(s->h2d, io.computed, 0));
+      SDG_CUDA_TRY(cudaStreamWaitEvent(s->h2d, io.downloaded, 0));
+    }
+    SDG_CUDA_TRY(cudaMemcpyAsync(io.q[0], q_in[r], bytes, cudaMemcpyHostToDevice, s->h2d));
+    const double* src[3] = {u[r], v[r], w[r]};
+    void* dst[3] = {io.u, io.v, io.w};
+    for (int c = 0; c < 3; c++) {
+      if (s->prec != SDG_PREC_FP32) {
+        SDG_CUDA_TRY(cudaMemcpyAsync(dst[c], src[c], bytes, cudaMemcpyHostToDevice, s->h2d));
+      } else {
+        // FP64 staging through a free state buffer, narrowed on the device
+        SDG_CUDA_TRY(cudaMemcpyAsync(io.q[1], src[c], bytes, cudaMemcpyHostToDevice, s->h2d));
+        f64_to_f32_kernel<<<grid_for(s->ndof), 256, 0, s->h2d>>>(static_cast<float*>(dst[c]),
+                                                               io.q[1], s->ndof);
+        SDG_CUDA_TRY(cudaGetLastError());
+      }
+    }
+    SDG_CUDA_TRY(cudaEventRecord(io.uploaded, s->h2d));
+    SDG_CUDA_TRY(cudaStreamWaitEvent(s->comp, io.uploaded, 0));
+    int cur = 0;
+    for (int it = 0; it < nstep; it++) {
+      const int s0 = cur, s1 = (cur + 1) % 3, s2 = (cur + 2) % 3;
+      SDG_TRY(one_stage_on(s, 0, dt, io.q[s0], nullptr, io.q[s1], io.u, io.v, io.w, s->comp, false));
+      SDG_TRY(one_stage_on(s, 1, dt, io.q[s1], io.q[s0], io.q[s2], io.u, io.v, io.w, s->comp, false));
+      SDG_TRY(one_stage_on(s, 2, dt, io.q[s2], io.q[s0], io.q[s1], io.u, io.v, io.w, s->comp, false));
+      cur = s1;
+    }
+    SDG_CUDA_TRY(cudaEventRecord(io.computed, s->comp));
+    SDG_CUDA_TRY(cudaStreamWaitEvent(s->d2h, io.computed, 0));
+    SDG_CUDA_TRY(cudaMemcpyAsync(q_out[r], io.q[cur], bytes, cudaMemcpyDeviceToHost, s->d2h));
+    SDG_CUDA_TRY(cudaEventRecord(io.downloaded, s->d2h));
+  }
+  SDG_CUDA_TRY(cudaStreamSynchronize(s->h2d));
+  SDG_CUDA_TRY(cudaStreamSynchronize(s->comp));
+  SDG_CUDA_TRY(cudaStreamSynchronize(s->d2h));
   return SDG_OK;
 }
 

@@ -109,6 +109,9 @@ def _load() -> C.CDLL:
         "sdg_solver_step": ([_vp, _d, _i], _i),
         "sdg_solver_step_timed": ([_vp, _d, _i, C.POINTER(_d)], _i),
         "sdg_solver_download": ([_vp, _vp], _i),
+        "sdg_solver_solve_host_pipelined": ([_vp, _i, C.POINTER(_vp), C.POINTER(_vp),
+                                             C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), _d,
+                                             _i], _i),
         "sdg_solver_state_dev": ([_vp], _vp),
         "sdg_solver_tendency": ([_vp, _dp], _i),
         "sdg_solver_launches_per_step": ([_vp], _i),
@@ -367,6 +370,15 @@ class Solver:
         out = np.zeros(self.ndof) if out is None else out
         _check(lib.sdg_solver_download(self._h, out.ctypes.data), "sdg_solver_download")
         return out
+
+    def solve_host_pipelined(self, q_in, u, v, w, q_out, dt: float, nstep: int) -> None:
+        """Pipelined host-to-host solves; each argument is a list of host
+        pointers (e.g. PinnedArray.ptr) of Np*Ne doubles, one per request."""
+        n = len(q_in)
+        arr = [(_vp * n)(*lst) for lst in (q_in, u, v, w, q_out)]
+        _check(lib.sdg_solver_solve_host_pipelined(
+            self._h, n, *[C.cast(a, C.POINTER(_vp)) for a in arr], float(dt), int(nstep)),
+            "sdg_solver_solve_host_pipelined")
 
     def download_ptr(self, ptr: int) -> None:
         _check(lib.sdg_solver_download(self._h, ptr), "sdg_solver_download")

@@ -64,6 +64,25 @@ def test_solver_run_matches_oracle(p, dims, nstep, ic, prec):
     assert rel_l2(q, c.oracle_run(nstep)) <= TOL_RUN
 
 
+@pytest.mark.parametrize("prec", [sdg.PREC_FP64, sdg.PREC_FP32, sdg.PREC_FP64_EMU])
+def test_pipelined_host_solves_equal_plain_solves(prec):
+    dims, p, nstep = (3, 2, 4), 5, 3
+    cases = [Case(*dims, p, ic="blob", seed=W.BASE_SEED + 60 + r) for r in range(5)]
+    n = cases[0].nown
+    pins = [[sdg.PinnedArray(n) for _ in range(5)] for _ in cases]
+    for c, pa in zip(cases, pins):
+        for arr, src in zip(pa[:4], (c.q, c.u, c.v, c.w)):
+            arr.array[:] = src[:n]
+    s = solver_for(cases[0], prec=prec)
+    s.solve_host_pipelined([pa[0].ptr for pa in pins], [pa[1].ptr for pa in pins],
+                           [pa[2].ptr for pa in pins], [pa[3].ptr for pa in pins],
+                           [pa[4].ptr for pa in pins], cases[0].dt, nstep)
+    for c, pa in zip(cases, pins):
+        ref = solver_for(c, prec=prec)
+        ref.step(cases[0].dt, nstep)
+        assert np.array_equal(pa[4].array, ref.download())
+
+
 def test_solver_steps_compose():
     c = Case(3, 3, 2, 4, ic="blob")
     a = solver_for(c)
