@@ -153,6 +153,19 @@ int sdg_advect3d_eq_cal_tend_noalloc(double* dqdt, const double* q,
                                      int NfpTot, int Ne, int NeA, int opt,
                                      void* stream);
 
+/* mesh_setup (mod_mesh.f90:74-193) on the device for the periodic box
+ * [0,Lx]x[0,Ly]x[0,Lz]: fills caller-owned device arrays with the reference's
+ * VMapM, VMapP (NfpTot,Ne; 1-based, periodic faces pointing into the halo
+ * buffer in the reference's slot order), normal_fn (NfpTot,Ne,3), Escale
+ * (Np,Ne,3), Fscale (NfpTot,Ne), pos_en (Np,Ne,3) and halo_src_map
+ * (Nfp*Nhalo).  Any output may be NULL; x1D (host, Nq values) is needed only
+ * for pos_en.  The values equal a host mesh_setup bit for bit.  Synchronises
+ * `stream` before returning. */
+int sdg_mesh_setup_dev(int NeX, int NeY, int NeZ, int p, double Lx, double Ly,
+                       double Lz, const double* x1D, int* VMapM, int* VMapP,
+                       double* normal_fn, double* Escale, double* Fscale,
+                       double* pos_en, int* halo_src_map, void* stream);
+
 /* tensorprod_divlike_dirXYZ (mod_dg_optr_kernel.f90:62-136) over nelem
  * consecutive elements (nelem = 1 is the reference call made per element from
  * mod_advect3d_eq.f90:185-188).  Each array holds nelem blocks of Nq^3

@@ -100,6 +100,7 @@ def _load() -> C.CDLL:
         "sdg_tensorprod_Lift_hexahedral": ([_dp, _dp, _dp, _i, _i], _i),
         "sdg_tensorprod_Lift_hexahedral_dev": ([_vp, _vp, _vp, _i, _i, _vp], _i),
         "sdg_update_halo_dev": ([_vp, _vp, _i, _i, _i, _vp], _i),
+        "sdg_mesh_setup_dev": ([_i, _i, _i, _i, _d, _d, _d, _vp] + [_vp] * 7 + [_vp], _i),
         "sdg_rk_stage_dev": ([_vp, _vp, _vp, _i, _i, _i, _d, _vp], _i),
         "sdg_solver_create": ([C.POINTER(_vp), _i, _i, _i, _i, _d, _d, _d, _dp, _dp, _i, _i,
                                _vp], _i),

@@ -164,6 +164,60 @@ def test_dev_update_halo_and_rk_stage_match_oracle():
         assert np.max(np.abs(dqq.numpy() - ref)) <= 4e-16 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("dims,p", [((3, 2, 4), 3), ((1, 2, 3), 2), ((4, 4, 4), 7), ((2, 1, 1), 9)])
+def test_device_mesh_equals_reference_mesh(dims, p):
+    x, D, Dt, L = operators(p)
+    m = O.Mesh(*dims, p, x)
+    outs = {"VMapM": sdg.DeviceArray(n=m.VMapM.size, dtype=np.int32),
+            "VMapP": sdg.DeviceArray(n=m.VMapP.size, dtype=np.int32),
+            "normal_fn": sdg.DeviceArray(n=m.normal_fn.size),
+            "Escale": sdg.DeviceArray(n=m.Escale.size),
+            "Fscale": sdg.DeviceArray(n=m.Fscale.size),
+            "pos_en": sdg.DeviceArray(n=m.pos_en.size),
+            "halo_src_map": sdg.DeviceArray(n=m.halo_src_map.size, dtype=np.int32)}
+    st = sdg.lib.sdg_mesh_setup_dev(*dims, p, 1.0, 1.0, 1.0, x.ctypes.data,
+                                    *[outs[k].ptr for k in ("VMapM", "VMapP", "normal_fn", "Escale",
+                                                            "Fscale", "pos_en", "halo_src_map")],
+                                    None)
+    assert st == 0, sdg.lib.sdg_last_error()
+    for k, d in outs.items():
+        assert np.array_equal(d.numpy(), getattr(m, k)), k
+
+
+def test_device_only_dropin_path_matches_oracle():
+    """Mesh built on the device, then update_halo and cal_tend on device
+    arrays: the reference's whole per-stage sequence without host arrays."""
+    c = Case(3, 2, 2, 4, ic="blob")
+    m = c.mesh
+    vm = sdg.DeviceArray(n=m.VMapM.size, dtype=np.int32)
+    vp = sdg.DeviceArray(n=m.VMapP.size, dtype=np.int32)
+    nf = sdg.DeviceArray(n=m.normal_fn.size)
+    es = sdg.DeviceArray(n=m.Escale.size)
+    fs = sdg.DeviceArray(n=m.Fscale.size)
+    hm = sdg.DeviceArray(n=m.halo_src_map.size, dtype=np.int32)
+    assert sdg.lib.sdg_mesh_setup_dev(c.NeX, c.NeY, c.NeZ, c.p, 1.0, 1.0, 1.0, None, vm.ptr, vp.ptr,
+                                      nf.ptr, es.ptr, fs.ptr, None, hm.ptr, None) == 0
+    fields = []
+    for f in (c.q, c.u, c.v, c.w):
+        g = f.copy()
+        g[c.nown:] = 0.0  # halos are filled on the device
+        d = sdg.DeviceArray(g)
+        assert sdg.lib.sdg_update_halo_dev(d.ptr, hm.ptr, m.Np, m.Ne, m.NhaloNode, None) == 0
+        fields.append(d)
+    ops = [sdg.DeviceArray(a) for a in (c.D, c.Dt, c.Lift)]
+    out = sdg.DeviceArray(n=m.Np * m.NeA)
+    flux = sdg.DeviceArray(n=m.NfpTot * m.Ne)
+    err = sdg.DeviceArray(np.zeros(1, dtype=np.int32))
+    st = sdg.lib.sdg_advect3d_eq_cal_tend_dev(out.ptr, *[f.ptr for f in fields],
+                                              *[o.ptr for o in ops], vm.ptr, vp.ptr, nf.ptr,
+                                              es.ptr, fs.ptr, m.Nq, m.Np, m.NfpTot, m.Ne, m.NeA,
+                                              sdg.OPT_OPT1, flux.ptr, err.ptr, None)
+    assert st == 0
+    sdg.synchronize()
+    assert err.numpy()[0] == 0
+    assert rel_l2(out.numpy()[: c.nown], c.oracle_tend()) <= TOL_TEND
+
+
 def test_dev_cal_tend_sets_error_flag():
     c = Case(2, 2, 1, 2, ic="blob")
     m = c.mesh
