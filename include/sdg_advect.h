@@ -153,6 +153,12 @@ int sdg_advect3d_eq_cal_tend_noalloc(double* dqdt, const double* q,
                                      int NfpTot, int Ne, int NeA, int opt,
                                      void* stream);
 
+/* minval / maxval of n device doubles (main.f90:76-79 prints them for
+ * q(:,1:Ne)), exact and independent of reduction order; host results.
+ * Synchronises `stream`. */
+int sdg_minmax_dev(const double* q, long long n, double* qmin, double* qmax,
+                   void* stream);
+
 /* mesh_setup (mod_mesh.f90:74-193) on the device for the periodic box
  * [0,Lx]x[0,Ly]x[0,Lz]: fills caller-owned device arrays with the reference's
  * VMapM, VMapP (NfpTot,Ne; 1-based, periodic faces pointing into the halo
@@ -182,6 +188,44 @@ int sdg_tensorprod_divlike_dirXYZ_dev(double* vec_out_x, double* vec_out_y,
                                       const double* vec_in_y,
                                       const double* vec_in_z, int Nq,
                                       int nelem, int opt, void* stream);
+
+/* element_operation_kernel_matvec_gradlike_dirXYZ_P* (opt1 erb:166-219) over
+ * nelem elements: the x, y and z derivatives of ONE field, vec_out_x =
+ * Mat along i, vec_out_y / vec_out_z = Mat_tr along j / k, running sums.
+ * The template's z direction starts with vec_in(i,1,k)*Mat_tr(1,j)
+ * (erb:209), a typo; this computes the consistent sum_l vec_in(i,j,l) *
+ * Mat_tr(l,k). */
+int sdg_tensorprod_gradlike_dirXYZ(double* vec_out_x, double* vec_out_y,
+                                   double* vec_out_z, const double* Mat,
+                                   const double* Mat_tr, const double* vec_in,
+                                   int Nq, int nelem);
+int sdg_tensorprod_gradlike_dirXYZ_dev(double* vec_out_x, double* vec_out_y,
+                                       double* vec_out_z, const double* Mat,
+                                       const double* Mat_tr,
+                                       const double* vec_in, int Nq, int nelem,
+                                       void* stream);
+
+/* element_operation_kernel_matvec_divlike_dirXYZ_var5_P* (opt1
+ * erb:347-465): the divlike contraction of 5 variables per element, in the
+ * OPT1 summation order (three partial sums for p > 7).  Each array holds
+ * nelem blocks of (Nq,Nq,Nq,5) values, outputs in the same layout.  The
+ * template's y output index, j + (kv-1)*5*Nq (erb:400), runs past
+ * vec_out_y for kv > 1; this writes vec_out_y(i,j,k,v) like x and z. */
+int sdg_tensorprod_divlike_dirXYZ_var5(double* vec_out_x, double* vec_out_y,
+                                       double* vec_out_z, const double* Mat,
+                                       const double* Mat_tr,
+                                       const double* vec_in_x,
+                                       const double* vec_in_y,
+                                       const double* vec_in_z, int Nq,
+                                       int nelem);
+int sdg_tensorprod_divlike_dirXYZ_var5_dev(double* vec_out_x,
+                                           double* vec_out_y,
+                                           double* vec_out_z, const double* Mat,
+                                           const double* Mat_tr,
+                                           const double* vec_in_x,
+                                           const double* vec_in_y,
+                                           const double* vec_in_z, int Nq,
+                                           int nelem, void* stream);
 
 /* tensorprod_Lift_hexahedral (mod_dg_optr_kernel.f90:139-190) over nelem
  * elements: vec_in holds nelem blocks of (Nq,Nq,6), vec_out nelem blocks of
@@ -259,6 +303,16 @@ int sdg_solver_solve_host_pipelined(sdg_solver* s, int count,
                                     double* const* q_out, double dt, int nstep);
 /* Device pointer of the current state q (Np*Ne doubles). */
 const double* sdg_solver_state_dev(const sdg_solver* s);
+/* minval / maxval of the current state over owned DOFs (main.f90:76-79),
+ * exact.  Synchronises the solver stream. */
+int sdg_solver_minmax(sdg_solver* s, double* qmin, double* qmax);
+/* The time loop with its diagnostic output (main.f90:51-80): nstep steps;
+ * after each step istep (1-based) with istep % output_interval == 0 the
+ * min and max of q are written to records[2k], records[2k+1] for the k-th
+ * such step (2 * (nstep / output_interval) doubles).  The loop does not wait
+ * for the host between steps; synchronises before returning. */
+int sdg_solver_run(sdg_solver* s, double dt, int nstep, int output_interval,
+                   double* records);
 /* Evaluates the tendency of the current state into dqdt (owned part,
  * host memory), the fused-kernel analogue of advect3d_eq_cal_tend. */
 int sdg_solver_tendency(sdg_solver* s, double* dqdt);

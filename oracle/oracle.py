@@ -51,6 +51,8 @@ def lib():
         L.sdgo_cal_elembnd_flux.argtypes = [_dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp, _dp, i, i, i, i]
         L.sdgo_divlike.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, i, i]
         L.sdgo_lift.argtypes = [_dp, _dp, _dp, i]
+        L.sdgo_gradlike.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, i]
+        L.sdgo_divlike_var5.argtypes = [_dp] * 8 + [i]
         L.sdgo_cal_dqdt.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                     i, i, i, i, i, i]
         L.sdgo_cal_tend.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip,
@@ -148,6 +150,23 @@ def divlike(D, Dt, fx, fy, fz, Nq, opt=OPT1):
     ox, oy, oz = np.zeros(Np), np.zeros(Np), np.zeros(Np)
     lib().sdgo_divlike(ox, oy, oz, D, Dt, np.ascontiguousarray(fx), np.ascontiguousarray(fy),
                        np.ascontiguousarray(fz), Nq, opt)
+    return ox, oy, oz
+
+
+def gradlike(D, Dt, f, Nq):
+    """gradlike_dirXYZ of one element's field (erb:166-219, z along k)."""
+    Np = Nq ** 3
+    ox, oy, oz = np.zeros(Np), np.zeros(Np), np.zeros(Np)
+    lib().sdgo_gradlike(ox, oy, oz, D, Dt, np.ascontiguousarray(f, dtype=np.float64), Nq)
+    return ox, oy, oz
+
+
+def divlike_var5(D, Dt, fx, fy, fz, Nq):
+    """divlike_dirXYZ_var5 of one element, (Nq,Nq,Nq,5) arrays (erb:347-465)."""
+    n = 5 * Nq ** 3
+    ox, oy, oz = np.zeros(n), np.zeros(n), np.zeros(n)
+    lib().sdgo_divlike_var5(ox, oy, oz, D, Dt, *[np.ascontiguousarray(a, dtype=np.float64)
+                                                 for a in (fx, fy, fz)], Nq)
     return ox, oy, oz
 
 

@@ -369,6 +369,49 @@ void sdgo_divlike(double* out_x, double* out_y, double* out_z, const double* D,
             sdgo_line(in_z + i + j * Nq, Nq2, D_tr + (long)k * Nq, 1, Nq, opt);
 }
 
+/* element_operation_kernel_matvec_gradlike_dirXYZ_P<p>
+ * (mod_dg_optr_kernel_opt1.F90.erb:166-219): x, y, z contractions of one
+ * field, each a running sum from the l = 1 product (the template has no
+ * three-way split).  The template's z direction begins with
+ * vec_in(i,1,k)*Mat_tr(1,j) (erb:209), a typo for vec_in(i,j,1)*Mat_tr(1,k);
+ * this restatement uses the consistent sum over l of vec_in(i,j,l) *
+ * Mat_tr(l,k). */
+static double sdgo_line_run(const double* a, long sa, const double* b, long sb, int Nq) {
+  double s = a[0] * b[0];
+  for (int l = 1; l < Nq; l++) s = s + a[l * sa] * b[l * sb];
+  return s;
+}
+
+void sdgo_gradlike(double* out_x, double* out_y, double* out_z, const double* D,
+                   const double* D_tr, const double* in, int Nq) {
+  const long Nq2 = (long)Nq * Nq;
+  for (long jk = 0; jk < Nq2; jk++)
+    for (int i = 0; i < Nq; i++)
+      out_x[i + jk * Nq] = sdgo_line_run(D + i, Nq, in + jk * Nq, 1, Nq);
+  for (int k = 0; k < Nq; k++)
+    for (int j = 0; j < Nq; j++)
+      for (int i = 0; i < Nq; i++) {
+        out_y[i + j * Nq + k * Nq2] =
+            sdgo_line_run(in + i + k * Nq2, Nq, D_tr + (long)j * Nq, 1, Nq);
+        out_z[i + j * Nq + k * Nq2] =
+            sdgo_line_run(in + i + j * Nq, Nq2, D_tr + (long)k * Nq, 1, Nq);
+      }
+}
+
+/* element_operation_kernel_matvec_divlike_dirXYZ_var5_P<p> (erb:347-465):
+ * five variables, (Nq,Nq,Nq,5) per array, each the OPT1-order divlike.  The
+ * template's y output index j + (kv-1)*5*Nq (erb:400) lies outside
+ * vec_out_y for kv > 1; the output here is vec_out_y(i,j,k,v), the layout of
+ * the x and z outputs. */
+void sdgo_divlike_var5(double* out_x, double* out_y, double* out_z, const double* D,
+                       const double* D_tr, const double* in_x, const double* in_y,
+                       const double* in_z, int Nq) {
+  const long Np = (long)Nq * Nq * Nq;
+  for (int v = 0; v < 5; v++)
+    sdgo_divlike(out_x + v * Np, out_y + v * Np, out_z + v * Np, D, D_tr, in_x + v * Np,
+                 in_y + v * Np, in_z + v * Np, Nq, SDGO_OPT1);
+}
+
 /* tensorprod_Lift_hexahedral, mod_dg_optr_kernel.f90:262-288 */
 void sdgo_lift(double* out, const double* Lift, const double* in, int Nq) {
   const long Nq2 = (long)Nq * Nq, Np = Nq2 * Nq;

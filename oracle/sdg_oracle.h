@@ -81,6 +81,17 @@ void sdgo_divlike(double* out_x, double* out_y, double* out_z, const double* D,
                   const double* D_tr, const double* in_x, const double* in_y,
                   const double* in_z, int Nq, int opt);
 
+/* gradlike_dirXYZ for one element (mod_dg_optr_kernel_opt1.F90.erb:166-219),
+ * with the z direction contracted along k. */
+void sdgo_gradlike(double* out_x, double* out_y, double* out_z, const double* D,
+                   const double* D_tr, const double* in, int Nq);
+
+/* divlike_dirXYZ_var5 for one element (erb:347-465): 5 variables, OPT1
+ * order; arrays are (Nq,Nq,Nq,5). */
+void sdgo_divlike_var5(double* out_x, double* out_y, double* out_z, const double* D,
+                       const double* D_tr, const double* in_x, const double* in_y,
+                       const double* in_z, int Nq);
+
 /* tensorprod_Lift_hexahedral for one element (mod_dg_optr_kernel.f90:139-190,
  * :262-288; erb:134-157 has the same order). */
 void sdgo_lift(double* out, const double* Lift, const double* in, int Nq);

@@ -17,7 +17,7 @@ SDG_DECL_DROPIN(9) SDG_DECL_DROPIN(10) SDG_DECL_DROPIN(11) SDG_DECL_DROPIN(12)
 SDG_DECL_DROPIN(13) SDG_DECL_DROPIN(14) SDG_DECL_DROPIN(15)
 #undef SDG_DECL_DROPIN
 
-// what: 0 = cal_dqdt, 1 = divlike, 2 = lift (mod_dg_optr_kernel.f90:87-133
+// what: 0 = cal_dqdt, 1 = divlike, 2 = lift, 3 = gradlike (mod_dg_optr_kernel.f90:87-133
 // and :155-186 select the per-order kernel the same way).
 static int dropin(int p, int what, int opt, const void* args, cudaStream_t st) {
   switch (p) {
@@ -274,6 +274,91 @@ int sdg_tensorprod_divlike_dirXYZ(double* ox, double* oy, double* oz,
   SDG_CUDA_TRY(cudaMemcpy(oy, a.oy, 8 * n, cudaMemcpyDeviceToHost));
   SDG_CUDA_TRY(cudaMemcpy(oz, a.oz, 8 * n, cudaMemcpyDeviceToHost));
   return SDG_OK;
+}
+
+// gradlike_dirXYZ (erb:166-219): one input field, three outputs.
+int sdg_tensorprod_gradlike_dirXYZ_dev(double* ox, double* oy, double* oz, const double* Mat,
+                                       const double* Mat_tr, const double* in, int Nq,
+                                       int nelem, void* stream) {
+  SDG_TRY(check_order(Nq));
+  if (nelem < 0) return fail(SDG_ERR_INVALID_ARG, "nelem < 0");
+  if (nelem == 0) return SDG_OK;
+  if (!ox || !oy || !oz || !Mat || !Mat_tr || !in)
+    return fail(SDG_ERR_INVALID_ARG, "NULL device pointer");
+  DivArgs a{ox, oy, oz, Mat, Mat_tr, in, nullptr, nullptr, nelem};
+  return dropin(Nq - 1, 3, SDG_OPT_GENERAL, &a, as_stream(stream));
+}
+
+// divlike_dirXYZ_var5 (erb:347-465): five variables per element, each the
+// OPT1-order divlike contraction; the (Nq,Nq,Nq,5) element blocks make the
+// call the divlike kernel over 5*nelem consecutive Nq^3 blocks.
+int sdg_tensorprod_divlike_dirXYZ_var5_dev(double* ox, double* oy, double* oz,
+                                           const double* Mat, const double* Mat_tr,
+                                           const double* ix, const double* iy,
+                                           const double* iz, int Nq, int nelem,
+                                           void* stream) {
+  SDG_TRY(check_order(Nq));
+  if (nelem < 0 || nelem > 0x7fffffff / 5) return fail(SDG_ERR_INVALID_ARG, "bad nelem %d", nelem);
+  if (nelem == 0) return SDG_OK;
+  if (!ox || !oy || !oz || !Mat || !Mat_tr || !ix || !iy || !iz)
+    return fail(SDG_ERR_INVALID_ARG, "NULL device pointer");
+  DivArgs a{ox, oy, oz, Mat, Mat_tr, ix, iy, iz, 5 * nelem};
+  return dropin(Nq - 1, 1, SDG_OPT_OPT1, &a, as_stream(stream));
+}
+
+namespace {
+// Host-pointer wrapper shared by gradlike and var5: copies nin inputs of n
+// doubles and the two Nq x Nq matrices in, runs `what`, copies 3 outputs out.
+int host_contract(int what, double* ox, double* oy, double* oz, const double* Mat,
+                  const double* Mat_tr, const double* const* in, int nin, int Nq, int nblocks,
+                  int opt) {
+  SDG_TRY(require_device());
+  const size_t n = (size_t)Nq * Nq * Nq * nblocks, nD = (size_t)Nq * Nq;
+  Arena ar;
+  size_t o[8];
+  for (int t = 0; t < 3; t++) o[t] = ar.add(8 * n);
+  o[3] = ar.add(8 * nD);
+  o[4] = ar.add(8 * nD);
+  for (int t = 0; t < nin; t++) o[5 + t] = ar.add(8 * n);
+  SDG_TRY(ar.alloc());
+  SDG_CUDA_TRY(cudaMemcpy(ar.at<void>(o[3]), Mat, 8 * nD, cudaMemcpyHostToDevice));
+  SDG_CUDA_TRY(cudaMemcpy(ar.at<void>(o[4]), Mat_tr, 8 * nD, cudaMemcpyHostToDevice));
+  for (int t = 0; t < nin; t++)
+    SDG_CUDA_TRY(cudaMemcpy(ar.at<void>(o[5 + t]), in[t], 8 * n, cudaMemcpyHostToDevice));
+  DivArgs a{ar.at<double>(o[0]), ar.at<double>(o[1]), ar.at<double>(o[2]),
+            ar.at<double>(o[3]), ar.at<double>(o[4]), ar.at<double>(o[5]),
+            nin > 1 ? ar.at<double>(o[6]) : nullptr, nin > 2 ? ar.at<double>(o[7]) : nullptr,
+            nblocks};
+  SDG_TRY(dropin(Nq - 1, what, opt, &a, nullptr));
+  SDG_CUDA_TRY(cudaMemcpy(ox, a.ox, 8 * n, cudaMemcpyDeviceToHost));
+  SDG_CUDA_TRY(cudaMemcpy(oy, a.oy, 8 * n, cudaMemcpyDeviceToHost));
+  SDG_CUDA_TRY(cudaMemcpy(oz, a.oz, 8 * n, cudaMemcpyDeviceToHost));
+  return SDG_OK;
+}
+}  // namespace
+
+int sdg_tensorprod_gradlike_dirXYZ(double* ox, double* oy, double* oz, const double* Mat,
+                                   const double* Mat_tr, const double* in, int Nq, int nelem) {
+  SDG_TRY(check_order(Nq));
+  if (nelem < 0) return fail(SDG_ERR_INVALID_ARG, "nelem < 0");
+  if (nelem == 0) return SDG_OK;
+  if (!ox || !oy || !oz || !Mat || !Mat_tr || !in)
+    return fail(SDG_ERR_INVALID_ARG, "NULL host pointer");
+  const double* ins[1] = {in};
+  return host_contract(3, ox, oy, oz, Mat, Mat_tr, ins, 1, Nq, nelem, SDG_OPT_GENERAL);
+}
+
+int sdg_tensorprod_divlike_dirXYZ_var5(double* ox, double* oy, double* oz, const double* Mat,
+                                       const double* Mat_tr, const double* ix,
+                                       const double* iy, const double* iz, int Nq,
+                                       int nelem) {
+  SDG_TRY(check_order(Nq));
+  if (nelem < 0 || nelem > 0x7fffffff / 5) return fail(SDG_ERR_INVALID_ARG, "bad nelem %d", nelem);
+  if (nelem == 0) return SDG_OK;
+  if (!ox || !oy || !oz || !Mat || !Mat_tr || !ix || !iy || !iz)
+    return fail(SDG_ERR_INVALID_ARG, "NULL host pointer");
+  const double* ins[3] = {ix, iy, iz};
+  return host_contract(1, ox, oy, oz, Mat, Mat_tr, ins, 3, Nq, 5 * nelem, SDG_OPT_OPT1);
 }
 
 int sdg_tensorprod_Lift_hexahedral_dev(double* out, const double* Lift,

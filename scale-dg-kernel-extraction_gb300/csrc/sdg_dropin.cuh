@@ -171,6 +171,61 @@ int launch_dqdt_impl(const TendArgs& a, cudaStream_t st) {
   return SDG_OK;
 }
 
+// element_operation_kernel_matvec_gradlike_dirXYZ_P* (erb:166-219): the
+// three directional contractions of ONE field (a.ix; a.iy and a.iz unused),
+// always as a running sum over l (the template has no three-way split).  The
+// z direction contracts along k, Σ_l vec_in(i,j,l) Mat_tr(l,k); the
+// template's first z term, vec_in(i,1,k)*Mat_tr(1,j), is a typo and is not
+// reproduced.  The field is staged once per element, so a DOF costs one read
+// and three writes.
+template <int P>
+constexpr size_t gradlike_smem_bytes() {
+  using O = Ord<P>;
+  return sizeof(double) * (size_t)(2 * O::NQ2 + DropCfg<P>::EPB * O::NP);
+}
+
+template <int P>
+__global__ void __launch_bounds__(DropCfg<P>::THREADS) gradlike_kernel(const DivArgs a) {
+  using O = Ord<P>;
+  constexpr int NQ = O::NQ, NQ2 = O::NQ2, NP = O::NP, EPB = DropCfg<P>::EPB,
+                T = DropCfg<P>::THREADS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* sD = reinterpret_cast<double*>(smem_raw);
+  double* sDt = sD + NQ2;
+  double* f = sDt + NQ2;
+  const long long eb = (long long)blockIdx.x * EPB;
+  const int nloc = (int)min((long long)EPB, (long long)a.nelem - eb);
+  if (nloc <= 0) return;
+  for (int t = threadIdx.x; t < NQ2; t += T) {
+    sD[t] = a.D[t];
+    sDt[t] = a.Dt[t];
+  }
+  const long long g0 = eb * NP;
+  for (int t = threadIdx.x; t < nloc * NP; t += T) f[t] = a.ix[g0 + t];
+  __syncthreads();
+  for (int t = threadIdx.x; t < nloc * NP; t += T) {
+    const int le = t / NP;
+    const int n = t - le * NP;
+    const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
+    const double* fe = f + le * NP;
+    a.ox[g0 + t] = line_sum<NQ, false, NQ>(sD + i, fe + j * NQ + k * NQ2, 1);
+    a.oy[g0 + t] = line_sum<NQ, false, 1>(sDt + j * NQ, fe + i + k * NQ2, NQ);
+    a.oz[g0 + t] = line_sum<NQ, false, 1>(sDt + k * NQ, fe + i + j * NQ, NQ2);
+  }
+}
+
+template <int P>
+int launch_gradlike_impl(const DivArgs& a, cudaStream_t st) {
+  constexpr size_t smem = gradlike_smem_bytes<P>();
+  SDG_CUDA_TRY(cudaFuncSetAttribute(gradlike_kernel<P>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long long nblk = ((long long)a.nelem + DropCfg<P>::EPB - 1) / DropCfg<P>::EPB;
+  if (nblk == 0) return SDG_OK;
+  gradlike_kernel<P><<<(unsigned)nblk, DropCfg<P>::THREADS, smem, st>>>(a);
+  SDG_CUDA_TRY(cudaGetLastError());
+  return SDG_OK;
+}
+
 template <int P, bool SPLIT3>
 int launch_divlike_impl(const DivArgs& a, cudaStream_t st) {
   constexpr size_t smem = divlike_smem_bytes<P>();
@@ -211,6 +266,8 @@ int dropin_order(int what, int opt, const void* args, cudaStream_t st) {
       return split ? launch_divlike_impl<P, kCanSplit>(a, st)
                    : launch_divlike_impl<P, false>(a, st);
     }
+    case 3:
+      return launch_gradlike_impl<P>(*static_cast<const DivArgs*>(args), st);
     default: {
       const DivArgs& a = *static_cast<const DivArgs*>(args);
       // lift: ox = out, D = Lift, ix = in

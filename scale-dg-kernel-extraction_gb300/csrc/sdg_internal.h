@@ -71,6 +71,11 @@ struct StageArgs {
 
 // Fused stage launchers (sdg_stage_*.cu).  prec = SDG_PREC_*.
 int launch_stage(int p, int prec, int opt, const StageArgs& a, cudaStream_t st);
+
+// min / max of q[0..n) as order keys (see sdg_minmax.cu); resets both keys first.
+int minmax_launch(const double* q, long long n, unsigned long long* kmin, unsigned long long* kmax,
+                  cudaStream_t st);
+double minmax_key_to_double(unsigned long long k);
 // Dynamic shared memory the launcher uses for order p, to size opt-in limits.
 int stage_setup_attributes(int p, int prec, int opt);
 

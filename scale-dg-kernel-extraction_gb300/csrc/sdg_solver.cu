@@ -378,6 +378,46 @@ int sdg_solver_step_timed(sdg_solver* s, double dt, int nstep, double* ms) {
   return SDG_OK;
 }
 
+int sdg_solver_minmax(sdg_solver* s, double* qmin, double* qmax) {
+  if (!s || !qmin || !qmax) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  return sdg_minmax_dev(s->q[s->cur], s->ndof, qmin, qmax, s->stream);
+}
+
+// The reference's time loop with its diagnostic output (main.f90:51-80): nstep
+// steps, and after every step istep with istep % output_interval == 0 the
+// min / max of q over owned DOFs.  The reductions write order keys into a
+// device record array on the solver stream, so the loop never waits for the
+// host; one copy at the end returns all records.
+int sdg_solver_run(sdg_solver* s, double dt, int nstep, int output_interval, double* records) {
+  if (!s) return fail(SDG_ERR_INVALID_ARG, "NULL solver");
+  if (nstep < 0 || output_interval < 1)
+    return fail(SDG_ERR_INVALID_ARG, "nstep < 0 or output_interval < 1");
+  const int nout = nstep / output_interval;
+  if (nout > 0 && !records) return fail(SDG_ERR_INVALID_ARG, "NULL records");
+  unsigned long long* keys = nullptr;
+  if (nout > 0)
+    SDG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&keys),
+                                 2 * sizeof(unsigned long long) * (size_t)nout, s->stream));
+  int rc = SDG_OK;
+  for (int k = 0; k < nout && rc == SDG_OK; k++) {
+    rc = sdg_solver_step(s, dt, output_interval);
+    if (rc == SDG_OK) rc = minmax_launch(s->q[s->cur], s->ndof, keys + 2 * k, keys + 2 * k + 1,
+                                         s->stream);
+  }
+  if (rc == SDG_OK) rc = sdg_solver_step(s, dt, nstep - nout * output_interval);
+  std::vector<unsigned long long> hk(2 * (size_t)nout);
+  cudaError_t e = cudaSuccess;
+  if (rc == SDG_OK && nout > 0)
+    e = cudaMemcpyAsync(hk.data(), keys, hk.size() * sizeof(unsigned long long),
+                        cudaMemcpyDeviceToHost, s->stream);
+  if (keys) cudaFreeAsync(keys, s->stream);
+  if (rc != SDG_OK) return rc;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "sdg_solver_run", __FILE__, __LINE__);
+  for (size_t i = 0; i < hk.size(); i++) records[i] = minmax_key_to_double(hk[i]);
+  return SDG_OK;
+}
+
 int sdg_solver_tendency(sdg_solver* s, double* dqdt) {
   if (!s || !dqdt) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
   if (!s->dqdt) SDG_CUDA_TRY(cudaMalloc(&s->dqdt, 8 * (size_t)s->ndof));

@@ -97,9 +97,16 @@ def _load() -> C.CDLL:
         "sdg_advect3d_eq_cal_tend_dev": ([_vp] * 13 + [_i] * 6 + [_vp, _vp, _vp], _i),
         "sdg_tensorprod_divlike_dirXYZ": ([_dp] * 8 + [_i, _i], _i),
         "sdg_tensorprod_divlike_dirXYZ_dev": ([_vp] * 8 + [_i, _i, _i, _vp], _i),
+        "sdg_tensorprod_gradlike_dirXYZ": ([_dp] * 6 + [_i, _i], _i),
+        "sdg_tensorprod_gradlike_dirXYZ_dev": ([_vp] * 6 + [_i, _i, _vp], _i),
+        "sdg_tensorprod_divlike_dirXYZ_var5": ([_dp] * 8 + [_i, _i], _i),
+        "sdg_tensorprod_divlike_dirXYZ_var5_dev": ([_vp] * 8 + [_i, _i, _vp], _i),
         "sdg_tensorprod_Lift_hexahedral": ([_dp, _dp, _dp, _i, _i], _i),
         "sdg_tensorprod_Lift_hexahedral_dev": ([_vp, _vp, _vp, _i, _i, _vp], _i),
         "sdg_update_halo_dev": ([_vp, _vp, _i, _i, _i, _vp], _i),
+        "sdg_minmax_dev": ([_vp, C.c_longlong, _vp, _vp, _vp], _i),
+        "sdg_solver_minmax": ([_vp, _vp, _vp], _i),
+        "sdg_solver_run": ([_vp, _d, _i, _i, _vp], _i),
         "sdg_mesh_setup_dev": ([_i, _i, _i, _i, _d, _d, _d, _vp] + [_vp] * 7 + [_vp], _i),
         "sdg_rk_stage_dev": ([_vp, _vp, _vp, _i, _i, _i, _d, _vp], _i),
         "sdg_solver_create": ([C.POINTER(_vp), _i, _i, _i, _i, _d, _d, _d, _dp, _dp, _i, _i,
@@ -234,6 +241,28 @@ def tensorprod_divlike_dirXYZ(Mat, Mat_tr, vec_in_x, vec_in_y, vec_in_z, Nq):
     ox, oy, oz = np.zeros_like(ix), np.zeros_like(iy), np.zeros_like(iz)
     _check(lib.sdg_tensorprod_divlike_dirXYZ(ox, oy, oz, _f64(Mat), _f64(Mat_tr), ix, iy, iz,
                                              Nq, nelem), "tensorprod_divlike_dirXYZ")
+    return ox, oy, oz
+
+
+def tensorprod_gradlike_dirXYZ(Mat, Mat_tr, vec_in, Nq):
+    """gradlike_dirXYZ (opt1 erb:166-219) over len(vec_in)//Nq^3 elements."""
+    vi = _f64(vec_in)
+    nelem = vi.size // Nq ** 3
+    ox, oy, oz = np.zeros_like(vi), np.zeros_like(vi), np.zeros_like(vi)
+    _check(lib.sdg_tensorprod_gradlike_dirXYZ(ox, oy, oz, _f64(Mat), _f64(Mat_tr), vi, Nq,
+                                              nelem), "tensorprod_gradlike_dirXYZ")
+    return ox, oy, oz
+
+
+def tensorprod_divlike_dirXYZ_var5(Mat, Mat_tr, vec_in_x, vec_in_y, vec_in_z, Nq):
+    """divlike_dirXYZ_var5 (opt1 erb:347-465) over len(vec_in_x)//(5 Nq^3)
+    elements, each (Nq,Nq,Nq,5)."""
+    ix, iy, iz = _f64(vec_in_x), _f64(vec_in_y), _f64(vec_in_z)
+    nelem = ix.size // (5 * Nq ** 3)
+    ox, oy, oz = np.zeros_like(ix), np.zeros_like(iy), np.zeros_like(iz)
+    _check(lib.sdg_tensorprod_divlike_dirXYZ_var5(ox, oy, oz, _f64(Mat), _f64(Mat_tr), ix, iy,
+                                                  iz, Nq, nelem),
+           "tensorprod_divlike_dirXYZ_var5")
     return ox, oy, oz
 
 
@@ -380,6 +409,21 @@ class Solver:
         _check(lib.sdg_solver_solve_host_pipelined(
             self._h, n, *[C.cast(a, C.POINTER(_vp)) for a in arr], float(dt), int(nstep)),
             "sdg_solver_solve_host_pipelined")
+
+    def minmax(self):
+        """(min, max) of the current state (main.f90:76-79)."""
+        lo, hi = C.c_double(), C.c_double()
+        _check(lib.sdg_solver_minmax(self._h, C.byref(lo), C.byref(hi)), "sdg_solver_minmax")
+        return lo.value, hi.value
+
+    def run(self, dt: float, nstep: int, output_interval: int) -> np.ndarray:
+        """The reference's time loop with its min/max output: returns an
+        (nstep // output_interval, 2) array of (min, max) records."""
+        nout = nstep // output_interval if output_interval > 0 else 0
+        rec = np.zeros(2 * max(nout, 1))
+        _check(lib.sdg_solver_run(self._h, float(dt), int(nstep), int(output_interval),
+                                  rec.ctypes.data), "sdg_solver_run")
+        return rec[: 2 * nout].reshape(-1, 2)
 
     def download_ptr(self, ptr: int) -> None:
         _check(lib.sdg_solver_download(self._h, ptr), "sdg_solver_download")

@@ -94,3 +94,14 @@ def test_without_a_gpu_the_compute_path_fails_loudly():
     with pytest.raises(sdg.SdgError) as e:
         sdg.tensorprod_Lift_hexahedral(L, np.zeros(6 * 16), 4)
     assert e.value.status == sdg.ERR_NO_DEVICE
+
+
+def test_operator_variants_reject_bad_arguments():
+    """Argument checks run before any device work, so they hold without a GPU."""
+    x, D, Dt, L = operators(3)
+    with pytest.raises(sdg.SdgError):
+        sdg.tensorprod_gradlike_dirXYZ(D, Dt, np.zeros(64), 17)
+    assert sdg.lib.sdg_tensorprod_divlike_dirXYZ_var5_dev(None, None, None, None, None, None,
+                                                          None, None, 4, 1, None) != 0
+    assert sdg.lib.sdg_tensorprod_divlike_dirXYZ_var5_dev(None, None, None, None, None, None,
+                                                          None, None, 4, 0, None) == 0

@@ -1,6 +1,7 @@
 """GPU parity: every CUDA entry point against the CPU oracle on the same
 inputs, through the C ABI.  Tolerances: relative L2 <= 1e-12 per tendency and
 <= 1e-10 after nstep for the FP64 form; <= 1e-5 for the FP32-compute form."""
+import ctypes as C
 import glob
 import os
 
@@ -105,6 +106,48 @@ def test_dropin_cal_tend_matches_oracle(p, opt):
     ref = c.oracle_tend(O.OPT1 if opt == "OPT1" else O.GENERAL)
     assert rel_l2(dqdt[: c.nown], ref) <= TOL_TEND
     assert np.all(dqdt[c.nown:] == 7.0)  # only dqdt(:,1:Ne) is written
+
+
+@pytest.mark.parametrize("p", range(1, 16))
+def test_gradlike_matches_oracle(p):
+    x, D, Dt, L = operators(p)
+    Nq, Np = p + 1, (p + 1) ** 3
+    nel = 7
+    f = np.random.default_rng(300 + p).standard_normal(Np * nel)
+    got = sdg.tensorprod_gradlike_dirXYZ(D, Dt, f, Nq)
+    for e in range(nel):
+        ref = O.gradlike(D, Dt, f[e * Np:(e + 1) * Np], Nq)
+        for d in range(3):
+            assert rel_l2(got[d][e * Np:(e + 1) * Np], ref[d]) <= TOL_TEND
+    # device-pointer form on the same data gives the same bits
+    dev = [sdg.DeviceArray(n=Np * nel) for _ in range(3)]
+    dD, dDt, df = sdg.DeviceArray(D), sdg.DeviceArray(Dt), sdg.DeviceArray(f)
+    assert sdg.lib.sdg_tensorprod_gradlike_dirXYZ_dev(*[o.ptr for o in dev], dD.ptr, dDt.ptr,
+                                                      df.ptr, Nq, nel, None) == 0
+    for d in range(3):
+        assert np.array_equal(dev[d].numpy(), got[d])
+
+
+@pytest.mark.parametrize("p", [1, 4, 7, 8, 10, 15])
+def test_divlike_var5_matches_oracle(p):
+    x, D, Dt, L = operators(p)
+    Nq, Np = p + 1, (p + 1) ** 3
+    nel = 3
+    rng = np.random.default_rng(400 + p)
+    fx, fy, fz = (rng.standard_normal(5 * Np * nel) for _ in range(3))
+    got = sdg.tensorprod_divlike_dirXYZ_var5(D, Dt, fx, fy, fz, Nq)
+    for e in range(nel):
+        sl = slice(5 * Np * e, 5 * Np * (e + 1))
+        ref = O.divlike_var5(D, Dt, fx[sl], fy[sl], fz[sl], Nq)
+        for d in range(3):
+            assert rel_l2(got[d][sl], ref[d]) <= TOL_TEND
+    dev = [sdg.DeviceArray(n=5 * Np * nel) for _ in range(3)]
+    ins = [sdg.DeviceArray(a) for a in (D, Dt, fx, fy, fz)]
+    assert sdg.lib.sdg_tensorprod_divlike_dirXYZ_var5_dev(*[o.ptr for o in dev],
+                                                          *[i.ptr for i in ins], Nq, nel,
+                                                          None) == 0
+    for d in range(3):
+        assert np.array_equal(dev[d].numpy(), got[d])
 
 
 def test_dropin_rejects_out_of_range_vmap():
@@ -216,6 +259,50 @@ def test_device_only_dropin_path_matches_oracle():
     sdg.synchronize()
     assert err.numpy()[0] == 0
     assert rel_l2(out.numpy()[: c.nown], c.oracle_tend()) <= TOL_TEND
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 1000, 4097, 1 << 20])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_minmax_dev_exact(n, offset):
+    rng = np.random.default_rng(n + offset)
+    x = rng.standard_normal(n + offset) * 10.0 ** rng.integers(-5, 5, n + offset)
+    d = sdg.DeviceArray(x)
+    lo, hi = C.c_double(), C.c_double()
+    # offset 1 moves the start off a 16-byte boundary (the scalar-load path)
+    assert sdg.lib.sdg_minmax_dev(d.ptr + 8 * offset, n, C.byref(lo), C.byref(hi), None) == 0
+    assert lo.value == x[offset:].min() and hi.value == x[offset:].max()
+
+
+def test_minmax_dev_signs_and_infinities():
+    x = np.array([3.0, -0.5, np.inf, -np.inf, 1e-300, -1e-300, 0.0])
+    d = sdg.DeviceArray(x)
+    lo, hi = C.c_double(), C.c_double()
+    assert sdg.lib.sdg_minmax_dev(d.ptr, x.size, C.byref(lo), C.byref(hi), None) == 0
+    assert lo.value == -np.inf and hi.value == np.inf
+    assert sdg.lib.sdg_minmax_dev(d.ptr + 8 * 4, 3, C.byref(lo), C.byref(hi), None) == 0
+    assert lo.value == -1e-300 and hi.value == 1e-300
+
+
+@pytest.mark.parametrize("ic", ["sine", "blob"])
+def test_solver_run_minmax_records(ic):
+    c = Case(3, 2, 2, 3, ic=ic)
+    nstep, every = 7, 2
+    ref = O.run(c.mesh, c.q.copy(), c.u, c.v, c.w, c.D, c.Dt, c.Lift, c.dt, nstep, minmax=True)
+    s = solver_for(c)
+    rec = s.run(c.dt, nstep, every)
+    assert rec.shape == (nstep // every, 2)
+    want = ref[every - 1 :: every][: nstep // every]
+    assert np.allclose(rec, want, rtol=1e-12, atol=1e-14 * np.abs(want).max())
+    q = s.download()
+    # the state after the loop is the plain stepper's, and the last record is
+    # its exact min/max after step 6
+    s2 = solver_for(c)
+    s2.step(c.dt, 6)
+    q6 = s2.download()
+    assert rec[-1, 0] == q6.min() and rec[-1, 1] == q6.max()
+    assert s2.minmax() == (q6.min(), q6.max())
+    s2.step(c.dt, 1)
+    assert np.array_equal(q, s2.download())
 
 
 def test_dev_cal_tend_sets_error_flag():

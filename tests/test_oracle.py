@@ -232,6 +232,72 @@ def test_general_equals_opt1_for_low_orders(p):
     assert np.array_equal(c.oracle_tend(O.OPT1), c.oracle_tend(O.GENERAL))
 
 
+# ---- gradlike / divlike_var5 (the next SCALE-DG operator kernels) ----------------------
+
+def _tensor_poly(x, a, b, c):
+    """x^a y^b z^c on the element's GLL nodes, (i,j,k) column-major, and its
+    three derivatives."""
+    X, Y, Z = np.meshgrid(x, x, x, indexing="ij")
+    def mono(t, m):
+        return t ** m
+    def dmono(t, m):
+        return m * t ** (m - 1) if m > 0 else np.zeros_like(t)
+    f = mono(X, a) * mono(Y, b) * mono(Z, c)
+    g = (dmono(X, a) * mono(Y, b) * mono(Z, c), mono(X, a) * dmono(Y, b) * mono(Z, c),
+         mono(X, a) * mono(Y, b) * dmono(Z, c))
+    return f.ravel(order="F"), [d.ravel(order="F") for d in g]
+
+
+@pytest.mark.parametrize("p", [1, 3, 7, 8, 12])
+def test_gradlike_differentiates_tensor_polynomials(p):
+    x, D, Dt, _ = operators(p)
+    for a, b, c in [(p, 0, 1), (1, p, 0), (0, 2 % (p + 1), p), (p, p, p)]:
+        f, g = _tensor_poly(x, a, b, c)
+        out = O.gradlike(D, Dt, f, p + 1)
+        for d in range(3):
+            assert np.max(np.abs(out[d] - g[d])) < 1e-11 * max(1.0, p ** 3), (a, b, c, d)
+
+
+@pytest.mark.parametrize("p", [2, 7, 9])
+def test_gradlike_z_contracts_along_k(p):
+    """The z output is sum_l f(i,j,l) D(k,l) (the template's erb:209 first term
+    vec_in(i,1,k)*Mat_tr(1,j) would break this)."""
+    x, D, Dt, _ = operators(p)
+    Nq = p + 1
+    f = np.random.default_rng(p).standard_normal(Nq ** 3)
+    F = f.reshape(Nq, Nq, Nq, order="F")
+    Dm = D.reshape(Nq, Nq, order="F")
+    ox, oy, oz = O.gradlike(D, Dt, f, Nq)
+    assert np.allclose(oz.reshape(Nq, Nq, Nq, order="F"), np.einsum("ijl,kl->ijk", F, Dm),
+                       rtol=0, atol=1e-13 * np.abs(Dm).max() * Nq)
+    assert np.allclose(oy.reshape(Nq, Nq, Nq, order="F"), np.einsum("ilk,jl->ijk", F, Dm),
+                       rtol=0, atol=1e-13 * np.abs(Dm).max() * Nq)
+
+
+@pytest.mark.parametrize("p", [3, 7])
+def test_gradlike_equals_divlike_of_one_field_for_low_orders(p):
+    x, D, Dt, _ = operators(p)
+    f = np.random.default_rng(7 + p).standard_normal((p + 1) ** 3)
+    g = O.gradlike(D, Dt, f, p + 1)
+    d = O.divlike(D, Dt, f, f, f, p + 1, O.OPT1)
+    for a, b in zip(g, d):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("p", [2, 7, 8, 13])
+def test_divlike_var5_is_five_opt1_divlikes(p):
+    x, D, Dt, _ = operators(p)
+    Np = (p + 1) ** 3
+    rng = np.random.default_rng(100 + p)
+    fx, fy, fz = (rng.standard_normal(5 * Np) for _ in range(3))
+    out = O.divlike_var5(D, Dt, fx, fy, fz, p + 1)
+    for v in range(5):
+        sl = slice(v * Np, (v + 1) * Np)
+        ref = O.divlike(D, Dt, fx[sl], fy[sl], fz[sl], p + 1, O.OPT1)
+        for a, b in zip(out, ref):
+            assert np.array_equal(a[sl], b)
+
+
 # ---- golden fixtures ---------------------------------------------------------------
 
 GOLDEN_FILES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
