@@ -205,6 +205,16 @@ int sdg_tensorprod_gradlike_dirXYZ_dev(double* vec_out_x, double* vec_out_y,
                                        const double* vec_in, int Nq, int nelem,
                                        void* stream);
 
+/* element_operation_kernel_matvec_dirX_P* / dirY_P* / dirZ_P* (opt1
+ * erb:51-129) over nelem elements, dir = 1, 2, 3: one running-sum
+ * contraction along i with Mat_x, or along j / k with the transposed
+ * Mat_y_tr / Mat_z_tr, exactly as the templates take them. */
+int sdg_element_matvec_dir(int dir, double* vec_out, const double* Mat,
+                           const double* vec_in, int Nq, int nelem);
+int sdg_element_matvec_dir_dev(int dir, double* vec_out, const double* Mat,
+                               const double* vec_in, int Nq, int nelem,
+                               void* stream);
+
 /* element_operation_kernel_matvec_divlike_dirXYZ_var5_P* (opt1
  * erb:347-465): the divlike contraction of 5 variables per element, in the
  * OPT1 summation order (three partial sums for p > 7).  Each array holds

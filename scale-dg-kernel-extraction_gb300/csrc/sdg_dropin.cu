@@ -361,6 +361,41 @@ int sdg_tensorprod_divlike_dirXYZ_var5(double* ox, double* oy, double* oz, const
   return host_contract(1, ox, oy, oz, Mat, Mat_tr, ins, 3, Nq, 5 * nelem, SDG_OPT_OPT1);
 }
 
+// element_operation_kernel_matvec_dirX / dirY / dirZ (erb:51-129): one
+// direction of the gradlike contraction; dir 1 takes Mat_x, dirs 2 and 3 the
+// transposed Mat_y_tr / Mat_z_tr, as the templates do.
+int sdg_element_matvec_dir_dev(int dir, double* vec_out, const double* Mat, const double* vec_in,
+                               int Nq, int nelem, void* stream) {
+  SDG_TRY(check_order(Nq));
+  if (dir < 1 || dir > 3) return fail(SDG_ERR_INVALID_ARG, "dir %d not in 1..3", dir);
+  if (nelem < 0) return fail(SDG_ERR_INVALID_ARG, "nelem < 0");
+  if (nelem == 0) return SDG_OK;
+  if (!vec_out || !Mat || !vec_in) return fail(SDG_ERR_INVALID_ARG, "NULL device pointer");
+  DivArgs a{dir == 1 ? vec_out : nullptr, dir == 2 ? vec_out : nullptr,
+            dir == 3 ? vec_out : nullptr, Mat, Mat, vec_in, nullptr, nullptr, nelem};
+  return dropin(Nq - 1, 3, SDG_OPT_GENERAL, &a, as_stream(stream));
+}
+
+int sdg_element_matvec_dir(int dir, double* vec_out, const double* Mat, const double* vec_in,
+                           int Nq, int nelem) {
+  SDG_TRY(check_order(Nq));
+  if (dir < 1 || dir > 3) return fail(SDG_ERR_INVALID_ARG, "dir %d not in 1..3", dir);
+  if (nelem < 0) return fail(SDG_ERR_INVALID_ARG, "nelem < 0");
+  if (nelem == 0) return SDG_OK;
+  if (!vec_out || !Mat || !vec_in) return fail(SDG_ERR_INVALID_ARG, "NULL host pointer");
+  SDG_TRY(require_device());
+  const size_t n = (size_t)Nq * Nq * Nq * nelem, nD = (size_t)Nq * Nq;
+  Arena ar;
+  const size_t oo = ar.add(8 * n), oM = ar.add(8 * nD), oi = ar.add(8 * n);
+  SDG_TRY(ar.alloc());
+  SDG_CUDA_TRY(cudaMemcpy(ar.at<void>(oM), Mat, 8 * nD, cudaMemcpyHostToDevice));
+  SDG_CUDA_TRY(cudaMemcpy(ar.at<void>(oi), vec_in, 8 * n, cudaMemcpyHostToDevice));
+  SDG_TRY(sdg_element_matvec_dir_dev(dir, ar.at<double>(oo), ar.at<double>(oM),
+                                     ar.at<double>(oi), Nq, nelem, nullptr));
+  SDG_CUDA_TRY(cudaMemcpy(vec_out, ar.at<void>(oo), 8 * n, cudaMemcpyDeviceToHost));
+  return SDG_OK;
+}
+
 int sdg_tensorprod_Lift_hexahedral_dev(double* out, const double* Lift,
                                        const double* in, int Nq, int nelem,
                                        void* stream) {

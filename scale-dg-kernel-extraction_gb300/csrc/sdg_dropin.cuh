@@ -177,7 +177,8 @@ int launch_dqdt_impl(const TendArgs& a, cudaStream_t st) {
 // z direction contracts along k, Σ_l vec_in(i,j,l) Mat_tr(l,k); the
 // template's first z term, vec_in(i,1,k)*Mat_tr(1,j), is a typo and is not
 // reproduced.  The field is staged once per element, so a DOF costs one read
-// and three writes.
+// and three writes.  A NULL output is skipped: with one output this is the
+// single-direction matvec_dirX / dirY / dirZ (erb:51-129).
 template <int P>
 constexpr size_t gradlike_smem_bytes() {
   using O = Ord<P>;
@@ -208,9 +209,9 @@ __global__ void __launch_bounds__(DropCfg<P>::THREADS) gradlike_kernel(const Div
     const int n = t - le * NP;
     const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
     const double* fe = f + le * NP;
-    a.ox[g0 + t] = line_sum<NQ, false, NQ>(sD + i, fe + j * NQ + k * NQ2, 1);
-    a.oy[g0 + t] = line_sum<NQ, false, 1>(sDt + j * NQ, fe + i + k * NQ2, NQ);
-    a.oz[g0 + t] = line_sum<NQ, false, 1>(sDt + k * NQ, fe + i + j * NQ, NQ2);
+    if (a.ox) a.ox[g0 + t] = line_sum<NQ, false, NQ>(sD + i, fe + j * NQ + k * NQ2, 1);
+    if (a.oy) a.oy[g0 + t] = line_sum<NQ, false, 1>(sDt + j * NQ, fe + i + k * NQ2, NQ);
+    if (a.oz) a.oz[g0 + t] = line_sum<NQ, false, 1>(sDt + k * NQ, fe + i + j * NQ, NQ2);
   }
 }
 

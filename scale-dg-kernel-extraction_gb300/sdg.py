@@ -97,6 +97,8 @@ def _load() -> C.CDLL:
         "sdg_advect3d_eq_cal_tend_dev": ([_vp] * 13 + [_i] * 6 + [_vp, _vp, _vp], _i),
         "sdg_tensorprod_divlike_dirXYZ": ([_dp] * 8 + [_i, _i], _i),
         "sdg_tensorprod_divlike_dirXYZ_dev": ([_vp] * 8 + [_i, _i, _i, _vp], _i),
+        "sdg_element_matvec_dir": ([_i, _dp, _dp, _dp, _i, _i], _i),
+        "sdg_element_matvec_dir_dev": ([_i, _vp, _vp, _vp, _i, _i, _vp], _i),
         "sdg_tensorprod_gradlike_dirXYZ": ([_dp] * 6 + [_i, _i], _i),
         "sdg_tensorprod_gradlike_dirXYZ_dev": ([_vp] * 6 + [_i, _i, _vp], _i),
         "sdg_tensorprod_divlike_dirXYZ_var5": ([_dp] * 8 + [_i, _i], _i),
@@ -242,6 +244,16 @@ def tensorprod_divlike_dirXYZ(Mat, Mat_tr, vec_in_x, vec_in_y, vec_in_z, Nq):
     _check(lib.sdg_tensorprod_divlike_dirXYZ(ox, oy, oz, _f64(Mat), _f64(Mat_tr), ix, iy, iz,
                                              Nq, nelem), "tensorprod_divlike_dirXYZ")
     return ox, oy, oz
+
+
+def element_matvec_dir(dir: int, Mat, vec_in, Nq):
+    """matvec_dirX/Y/Z (opt1 erb:51-129), dir 1..3, over len(vec_in)//Nq^3
+    elements; Mat is Mat_x, Mat_y_tr or Mat_z_tr."""
+    vi = _f64(vec_in)
+    out = np.zeros_like(vi)
+    _check(lib.sdg_element_matvec_dir(int(dir), out, _f64(Mat), vi, Nq, vi.size // Nq ** 3),
+           "element_matvec_dir")
+    return out
 
 
 def tensorprod_gradlike_dirXYZ(Mat, Mat_tr, vec_in, Nq):

@@ -105,3 +105,6 @@ def test_operator_variants_reject_bad_arguments():
                                                           None, None, 4, 1, None) != 0
     assert sdg.lib.sdg_tensorprod_divlike_dirXYZ_var5_dev(None, None, None, None, None, None,
                                                           None, None, 4, 0, None) == 0
+    with pytest.raises(sdg.SdgError):
+        sdg.element_matvec_dir(4, D, np.zeros(64), 4)
+    assert sdg.lib.sdg_element_matvec_dir_dev(0, None, None, None, 4, 1, None) != 0

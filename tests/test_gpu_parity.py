@@ -128,6 +128,22 @@ def test_gradlike_matches_oracle(p):
         assert np.array_equal(dev[d].numpy(), got[d])
 
 
+@pytest.mark.parametrize("p", [1, 6, 9, 15])
+def test_single_direction_matvecs_are_gradlike_components(p):
+    """matvec_dirX/Y/Z: running sums along one axis, the components of gradlike
+    (the oracle's gradlike is the z-along-k form)."""
+    x, D, Dt, L = operators(p)
+    Nq, Np = p + 1, (p + 1) ** 3
+    f = np.random.default_rng(500 + p).standard_normal(Np * 4)
+    full = sdg.tensorprod_gradlike_dirXYZ(D, Dt, f, Nq)
+    assert np.array_equal(sdg.element_matvec_dir(1, D, f, Nq), full[0])
+    assert np.array_equal(sdg.element_matvec_dir(2, Dt, f, Nq), full[1])
+    assert np.array_equal(sdg.element_matvec_dir(3, Dt, f, Nq), full[2])
+    ref = O.gradlike(D, Dt, f[:Np], Nq)
+    for d in range(3):
+        assert rel_l2(full[d][:Np], ref[d]) <= TOL_TEND
+
+
 @pytest.mark.parametrize("p", [1, 4, 7, 8, 10, 15])
 def test_divlike_var5_matches_oracle(p):
     x, D, Dt, L = operators(p)
