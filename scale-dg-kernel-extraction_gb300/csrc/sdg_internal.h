@@ -67,6 +67,10 @@ struct StageArgs {
   int b_is_one;         // b == 1 (stage 1): the kernels branch on integers,
   int a_nonzero;        // since an FP64 comparison also uses the FP64 pipe
   int tend_only;        // write dqdt instead of the RK update
+  // even-odd FP64 stage: per-direction factors of the D part (-c*Es_d) and
+  // of the lift part (-c*Fs_d/4) of the tables, c = b*dt (1 for tend_only);
+  // D then points at the 3-direction table built by the solver
+  double eo_sD[3], eo_sL[3];
 };
 
 // Fused stage launchers (sdg_stage_*.cu).  prec = SDG_PREC_*.

@@ -16,7 +16,7 @@ SDG_DECL_ORDER(13) SDG_DECL_ORDER(14) SDG_DECL_ORDER(15)
 int launch_stage(int p, int prec, int opt, const StageArgs& a, cudaStream_t st) {
   if (prec != SDG_PREC_FP64 && prec != SDG_PREC_FP32 && prec != SDG_PREC_FP64_EMU)
     return fail(SDG_ERR_INVALID_ARG, "unknown precision %d", prec);
-  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1)
+  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1 && opt != SDG_OPT_EVENODD)
     return fail(SDG_ERR_BAD_OPTTYPE, "unknown DGOptrKernel type %d", opt);
   switch (p) {
     case 1: return launch_stage_p1(prec, opt, a, st);

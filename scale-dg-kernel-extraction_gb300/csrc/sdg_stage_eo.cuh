@@ -1,0 +1,245 @@
+// Fused FP64 RK-stage kernel with the even-odd factorisation of the 1D
+// operators (opt type SDG_OPT_EVENODD).
+//
+// On GB300 the FP64 pipe runs at 1/64 of the FP32 rate, so the plain FP64
+// stage is bound by its count of FP64 instructions, not by HBM.  This body
+// computes the same tendency and stage update as stage_block<P, double> with
+// about 30 % fewer FP64 instructions per node:
+//
+//  * Centro-antisymmetry of the GLL differentiation matrix,
+//    D(N-1-i, N-1-l) = -D(i, l), splits a line's N-term sums into pairs:
+//    with S(l) = F(l) + F(N-1-l) and Δ(l) = F(l) - F(N-1-l), l < N/2,
+//        e_i = Σ_l E(i,l) S(l) [+ D(i,mid) F(mid)],  o_i = Σ_l O(i,l) Δ(l),
+//        out(i) = e_i + o_i,   out(N-1-i) = o_i - e_i,
+//    where E / O are the half-sums / half-differences of D's columns l and
+//    N-1-l.  A line of N outputs costs N²/2 + 2N operations instead of N².
+//  * The lift of a face is a 1D column along the face normal, constant over
+//    the tangential nodes, and the + face's column is the mirror of the -
+//    face's (Lift_mat of operator_data/p*.dat has both properties to
+//    rounding).  With gs = g- + g+ and gd = g- - g+ the two faces of a line
+//    join the same pairs: e_i += B(i) gd, o_i += A(i) gs.
+//  * Escale, the stage's b*dt and the minus sign of dqdt are folded into the
+//    tables when a block stages them, and 0.5*Fscale into the lift columns,
+//    so a node's increment is the plain sum of its three line results and
+//    the RK update is q_out = b*q + inc (+ a*q0).
+//  * The face flux 0.5 Fs (qP VelP - qM VelM - α (qP - qM)) is formed as
+//    qP (2VelP - 2α) - qM (2VelM - 2α) with 2α = |uP + uM| (the normal sign
+//    applied through the constant ±2): five FP64 operations per face node.
+//
+// Thread layout: phase 0 and the face flux run one thread per node / face
+// node as in stage_block; the three contraction phases run one thread per
+// line (N² lines per element and direction).  The x phase writes its line
+// results over F_x, the y phase adds into them and the z phase finishes the
+// node: every phase touches only its own line's nodes, and a barrier
+// separates the phases.
+//
+// The summation order is neither GENERAL's nor OPT1's; the result agrees
+// with both to rounding (the parity tests hold it to the same tolerance).
+// The host builds the E / O / lift tables only after checking the operator
+// symmetries; operators without them are refused for this opt type.
+#pragma once
+
+#include "sdg_stage.cuh"
+
+namespace sdg {
+
+template <int P>
+struct EoShape {
+  static constexpr int N = P + 1;
+  static constexpr int H = N / 2;          // pairs (l, N-1-l)
+  static constexpr int HR = (N + 1) / 2;   // output rows incl. the middle row
+  static constexpr int ODD = N & 1;
+  static constexpr int OFF_E = 0;                      // E(i,l), i < H, l < H
+  static constexpr int OFF_O = H * H;                  // O(i,l), i < HR, l < H
+  static constexpr int OFF_DM = OFF_O + HR * H;        // D(i,mid), i < H (odd N)
+  static constexpr int OFF_A = OFF_DM + ODD * H;       // lift sym part, i < HR
+  static constexpr int OFF_B = OFF_A + HR;             // lift antisym part, i < H
+  static constexpr int TE = OFF_B + H;                 // entries per direction
+};
+
+template <int P>
+struct EoCfg {
+  static constexpr int THREADS = 256;
+  static constexpr int EPB = (256 / Ord<P>::NQ2) > 0 ? 256 / Ord<P>::NQ2 : 1;
+};
+
+template <int P>
+__host__ __device__ constexpr size_t eo_smem_bytes() {
+  using O = Ord<P>;
+  return sizeof(double) *
+             (size_t)(3 * EoShape<P>::TE + EoCfg<P>::EPB * (4 * O::NP + O::NFT)) +
+         sizeof(int) * 6 * EoCfg<P>::EPB;
+}
+
+__device__ __forceinline__ double abs_bits(double x) {
+  return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
+}
+
+// One line: F (stride S) holds the line's N volume fluxes, T the direction's
+// scaled tables, gm / gp the face fluxes of the line's - and + faces.  The
+// N results go to emit(m, value) after all reads of F.
+template <int P, int S, typename Emit>
+__device__ __forceinline__ void eo_line(const double* F, const double* __restrict__ T, double gm,
+                                        double gp, Emit&& emit) {
+  using Sh = EoShape<P>;
+  constexpr int N = Sh::N, H = Sh::H;
+  double s[H], d[H];
+#pragma unroll
+  for (int l = 0; l < H; l++) {
+    const double lo = F[l * S], hi = F[(N - 1 - l) * S];
+    s[l] = lo + hi;
+    d[l] = lo - hi;
+  }
+  double fm = 0.0;
+  if constexpr (Sh::ODD != 0) fm = F[H * S];
+  const double gs = gm + gp, gd = gm - gp;
+  // rows unrolled up to p = 7; above that a rolled loop keeps the 2H line
+  // values and the row sums within the register budget
+  constexpr int kRowUnroll = (N <= 8) ? H : 1;
+#pragma unroll kRowUnroll
+  for (int i = 0; i < H; i++) {
+    double e = T[Sh::OFF_E + i * H] * s[0];
+#pragma unroll
+    for (int l = 1; l < H; l++) e = fma(T[Sh::OFF_E + i * H + l], s[l], e);
+    if constexpr (Sh::ODD != 0) e = fma(T[Sh::OFF_DM + i], fm, e);
+    e = fma(T[Sh::OFF_B + i], gd, e);
+    double o = T[Sh::OFF_O + i * H] * d[0];
+#pragma unroll
+    for (int l = 1; l < H; l++) o = fma(T[Sh::OFF_O + i * H + l], d[l], o);
+    o = fma(T[Sh::OFF_A + i], gs, o);
+    emit(i, e + o);
+    emit(N - 1 - i, o - e);
+  }
+  if constexpr (Sh::ODD != 0) {
+    double o = T[Sh::OFF_O + H * H] * d[0];
+#pragma unroll
+    for (int l = 1; l < H; l++) o = fma(T[Sh::OFF_O + H * H + l], d[l], o);
+    o = fma(T[Sh::OFF_A + H], gs, o);
+    emit(H, o);
+  }
+}
+
+template <int P>
+__global__ void __launch_bounds__(EoCfg<P>::THREADS) stage_eo_kernel(const StageArgs a) {
+  using O = Ord<P>;
+  using Sh = EoShape<P>;
+  constexpr int NQ = O::NQ, NQ2 = O::NQ2, NP = O::NP, NFP = O::NFP, NFT = O::NFT;
+  constexpr int EPB = EoCfg<P>::EPB, T = EoCfg<P>::THREADS, TE = Sh::TE;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* sT = reinterpret_cast<double*>(smem_raw);  // 3 directions x TE
+  const long long eb = a.elem_begin + (long long)blockIdx.x * EPB;
+  const long long eend = a.elem_begin + a.elem_count;
+  const int nloc = (int)((eend - eb) < EPB ? (eend - eb) : EPB);
+  if (nloc <= 0) return;
+  double* sq = sT + 3 * TE;
+  double* sFx = sq + nloc * NP;  // F_x, then the running sum of the line results
+  double* sFy = sFx + nloc * NP;
+  double* sFz = sFy + nloc * NP;
+  double* sf = sFz + nloc * NP;
+  int* snb = reinterpret_cast<int*>(sf + nloc * NFT);
+
+  const double* __restrict__ qin = a.q_in;
+  const double* __restrict__ gu = static_cast<const double*>(a.u);
+  const double* __restrict__ gv = static_cast<const double*>(a.v);
+  const double* __restrict__ gw = static_cast<const double*>(a.w);
+  const double* __restrict__ tab = static_cast<const double*>(a.D);
+  const long long g0 = eb * NP;
+
+  // phase 0: scaled tables, neighbours, q and F_d = q * u_d
+  for (int t = threadIdx.x; t < 3 * TE; t += T) {
+    const int dir = t / TE, w = t - dir * TE;
+    sT[t] = tab[t] * (w < Sh::OFF_A ? a.eo_sD[dir] : a.eo_sL[dir]);
+  }
+  for (int t = threadIdx.x; t < 6 * nloc; t += T)
+    snb[t] = (int)neighbor(a.box, eb + t / 6, t % 6);
+  for (int t = threadIdx.x; t < nloc * NP; t += T) {
+    const double qq = qin[g0 + t];
+    sq[t] = qq;
+    sFx[t] = qq * gu[g0 + t];
+    sFy[t] = qq * gv[g0 + t];
+    sFz[t] = qq * gw[g0 + t];
+  }
+  __syncthreads();
+
+  // phase 1: face fluxes qP (2VelP - 2α) - qM (2VelM - 2α), unscaled
+  for (int t = threadIdx.x; t < nloc * NFT; t += T) {
+    const int le = t / NFT;
+    const int r = t - le * NFT;
+    const int f = r / NFP;
+    const int fp = r - f * NFP;
+    int nM, nP, axis, sg;
+    face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sg);
+    const long long gM = g0 + (long long)le * NP + nM;
+    const long long gP = (long long)snb[6 * le + f] * NP + nP;
+    const double* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
+    const double uM = gvel[gM], uP = gvel[gP];
+    const double qM = sq[le * NP + nM];
+    const double qP = qin[gP];
+    const double a2 = abs_bits(uP + uM);
+    const double tw = (sg > 0) ? 2.0 : -2.0;
+    const double tP = fma(tw, uP, -a2);
+    const double tM = fma(tw, uM, -a2);
+    sf[le * NFT + r] = fma(qP, tP, -(qM * tM));
+  }
+  __syncthreads();
+
+  // phase 2x: lines along i, faces -x (3) and +x (1); results over F_x
+  for (int t = threadIdx.x; t < nloc * NQ2; t += T) {
+    const int le = t / NQ2, r = t - le * NQ2;
+    double* F = sFx + le * NP + r * NQ;
+    const double* fl = sf + le * NFT + r;
+    eo_line<P, 1>(F, sT, fl[3 * NFP], fl[1 * NFP], [&](int m, double v) { F[m] = v; });
+  }
+  __syncthreads();
+
+  // phase 2y: lines along j, faces -y (0) and +y (2); added into the sums
+  for (int t = threadIdx.x; t < nloc * NQ2; t += T) {
+    const int le = t / NQ2, r = t - le * NQ2;
+    const int off = le * NP + (r % NQ) + (r / NQ) * NQ2;
+    double* acc = sFx + off;
+    const double* fl = sf + le * NFT + r;
+    eo_line<P, NQ>(sFy + off, sT + TE, fl[0], fl[2 * NFP],
+                   [&](int m, double v) { acc[m * NQ] += v; });
+  }
+  __syncthreads();
+
+  // phase 2z: lines along k, faces -z (4) and +z (5); finish the node and the
+  // RK update q_out = b*q + inc (+ a*q0)
+  for (int t = threadIdx.x; t < nloc * NQ2; t += T) {
+    const int le = t / NQ2, r = t - le * NQ2;
+    const int off = le * NP + r;
+    const double* fl = sf + le * NFT + r;
+    eo_line<P, NQ2>(sFz + off, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], [&](int m, double v) {
+      const int n = off + m * NQ2;
+      const double inc = sFx[n] + v;
+      const long long g = g0 + n;
+      if (a.tend_only) {
+        a.q_out[g] = inc;
+      } else {
+        const double qv = sq[n];
+        double res = a.b_is_one ? qv + inc : fma(a.b, qv, inc);
+        if (a.a_nonzero) res = fma(a.a, a.q0[g], res);
+        a.q_out[g] = res;
+      }
+    });
+  }
+}
+
+template <int P>
+int launch_stage_eo_impl(const StageArgs& a, cudaStream_t st) {
+  constexpr size_t smem = eo_smem_bytes<P>();
+  static bool attr_done = false;
+  if (!attr_done) {
+    SDG_CUDA_TRY(cudaFuncSetAttribute(stage_eo_kernel<P>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_done = true;
+  }
+  const long long nblk = (a.elem_count + EoCfg<P>::EPB - 1) / EoCfg<P>::EPB;
+  if (nblk <= 0) return SDG_OK;
+  if (nblk > 0x7fffffffLL) return fail(SDG_ERR_INVALID_ARG, "too many elements");
+  stage_eo_kernel<P><<<(unsigned)nblk, EoCfg<P>::THREADS, smem, st>>>(a);
+  SDG_CUDA_TRY(cudaGetLastError());
+  return SDG_OK;
+}
+
+}  // namespace sdg

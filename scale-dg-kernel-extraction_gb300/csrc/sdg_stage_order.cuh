@@ -4,15 +4,18 @@
 
 #include "sdg_stage.cuh"
 #include "sdg_stage_emu.cuh"
+#include "sdg_stage_eo.cuh"
 
 namespace sdg {
 
 template <int P>
 int launch_stage_order(int prec, int opt, const StageArgs& a, cudaStream_t st) {
   constexpr bool kCanSplit = (P > 7);
-  const bool split = kCanSplit && (opt == SDG_OPT_OPT1);
+  // EVENODD: its own FP64 body; the FP32 form runs the OPT1 order for it
+  const bool split = kCanSplit && (opt != SDG_OPT_GENERAL);
   if (prec == SDG_PREC_FP64_EMU) return launch_stage_emu_impl<P>(a, st);
   if (prec == SDG_PREC_FP64) {
+    if (opt == SDG_OPT_EVENODD) return launch_stage_eo_impl<P>(a, st);
     if (split) return launch_stage_impl<P, double, double, kCanSplit>(a, st);
     return launch_stage_impl<P, double, double, false>(a, st);
   }

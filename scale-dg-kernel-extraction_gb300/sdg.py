@@ -33,6 +33,7 @@ ERR_NO_DEVICE = -9
 
 OPT_GENERAL = 1
 OPT_OPT1 = 2
+OPT_EVENODD = 3  # solver only: even-odd FP64 stage
 PREC_FP64 = 0
 PREC_FP32 = 1
 PREC_FP64_EMU = 2

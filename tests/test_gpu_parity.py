@@ -32,13 +32,53 @@ def solver_for(c: Case, opt=sdg.OPT_OPT1, prec=sdg.PREC_FP64):
 
 
 @pytest.mark.parametrize("p", range(1, 16))
-@pytest.mark.parametrize("opt", [sdg.OPT_OPT1, sdg.OPT_GENERAL])
+@pytest.mark.parametrize("opt", [sdg.OPT_OPT1, sdg.OPT_GENERAL, sdg.OPT_EVENODD])
 def test_fused_stage_tendency_matches_oracle(p, opt):
     c = Case(*mesh_dims(p), p, ic="blob")
     s = solver_for(c, opt)
     dq = s.tendency()
-    ref = c.oracle_tend(opt)
+    ref = c.oracle_tend(sdg.OPT_GENERAL if opt == sdg.OPT_GENERAL else sdg.OPT_OPT1)
     assert rel_l2(dq, ref) <= TOL_TEND
+
+
+@pytest.mark.parametrize("p", [1, 2, 5, 7, 8, 15])
+def test_evenodd_tendency_sine_and_anisotropic_box(p):
+    """Even-odd stage: per-direction Escale / Fscale folding on a box with
+    three different element sizes, and the sine initial state."""
+    c = Case(*mesh_dims(p), p, ic="sine")
+    assert rel_l2(solver_for(c, sdg.OPT_EVENODD).tendency(), c.oracle_tend()) <= TOL_TEND
+    L = (1.0, 2.5, 0.4)
+    m = O.Mesh(c.NeX, c.NeY, c.NeZ, p, c.x1D, L=L)
+    ref = O.cal_tend(m, c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, O.OPT1)[: c.nown]
+    s = sdg.Solver(c.NeX, c.NeY, c.NeZ, p, c.D, c.Lift, L=L, opt=sdg.OPT_EVENODD)
+    n = c.nown
+    s.upload(c.q[:n], c.u[:n], c.v[:n], c.w[:n])
+    assert rel_l2(s.tendency(), ref) <= TOL_TEND
+
+
+@pytest.mark.parametrize("p,dims,nstep", [(3, (8, 8, 8), 100), (7, (4, 3, 2), 20),
+                                          (10, (2, 2, 2), 5), (1, (1, 2, 3), 30),
+                                          (2, (3, 1, 2), 10)])
+def test_evenodd_run_matches_oracle(p, dims, nstep):
+    c = Case(*dims, p, ic="blob")
+    s = solver_for(c, sdg.OPT_EVENODD)
+    s.step(c.dt, nstep)
+    assert rel_l2(s.download(), c.oracle_run(nstep)) <= TOL_RUN
+
+
+def test_evenodd_refuses_operators_without_centro_symmetry():
+    x, D, Dt, L = operators(4)
+    bad = D.copy()
+    bad[3] *= 1.0 + 1e-9
+    with pytest.raises(sdg.SdgError) as e:
+        sdg.Solver(2, 2, 2, 4, bad, L, opt=sdg.OPT_EVENODD)
+    assert e.value.status == sdg.ERR_INVALID_ARG
+    badL = L.copy()
+    badL[7] *= 1.0 + 1e-9
+    with pytest.raises(sdg.SdgError):
+        sdg.Solver(2, 2, 2, 4, D, badL, opt=sdg.OPT_EVENODD)
+    # the node bodies take any operator
+    sdg.Solver(2, 2, 2, 4, bad, badL, opt=sdg.OPT_OPT1)
 
 
 @pytest.mark.parametrize("p", range(1, 16))
@@ -379,6 +419,11 @@ def test_gpu_matches_golden_fixture(path):
     s2 = sdg.Solver(NeX, NeY, NeZ, p, g["D"], g["Lift"], opt=sdg.OPT_GENERAL)
     s2.upload(g["q"], g["u"], g["v"], g["w"])
     assert rel_l2(s2.tendency(), g["dqdt_general"]) <= TOL_TEND
+    s3 = sdg.Solver(NeX, NeY, NeZ, p, g["D"], g["Lift"], opt=sdg.OPT_EVENODD)
+    s3.upload(g["q"], g["u"], g["v"], g["w"])
+    assert rel_l2(s3.tendency(), g["dqdt_opt1"]) <= TOL_TEND
+    s3.step(float(g["dt"]), nstep)
+    assert rel_l2(s3.download(), g["q_final"]) <= TOL_RUN
 
 
 # ---- full-size properties (p=7, 32^3: 16.8M DOF) -------------------------------
@@ -392,11 +437,13 @@ def full_case():
                 dt=W.cfl_dt(N, N, N, p, u, v, w))
 
 
-@pytest.mark.parametrize("prec", [sdg.PREC_FP64, sdg.PREC_FP64_EMU])
-def test_full_size_tendency_matches_oracle(full_case, prec):
+@pytest.mark.parametrize("prec,opt", [(sdg.PREC_FP64, sdg.OPT_OPT1),
+                                      (sdg.PREC_FP64_EMU, sdg.OPT_OPT1),
+                                      (sdg.PREC_FP64, sdg.OPT_EVENODD)])
+def test_full_size_tendency_matches_oracle(full_case, prec, opt):
     f = full_case
     N, p = f["N"], f["p"]
-    s = sdg.Solver(N, N, N, p, f["D"], f["L"], precision=prec)
+    s = sdg.Solver(N, N, N, p, f["D"], f["L"], opt=opt, precision=prec)
     s.upload(f["q"], f["u"], f["v"], f["w"])
     dq = s.tendency()
     m = O.Mesh(N, N, N, p, f["x"])
@@ -407,11 +454,13 @@ def test_full_size_tendency_matches_oracle(full_case, prec):
     assert rel_l2(dq, ref) <= TOL_TEND
 
 
-@pytest.mark.parametrize("prec", [sdg.PREC_FP64, sdg.PREC_FP64_EMU])
-def test_full_size_mass_conservation_and_shift_invariance(full_case, prec):
+@pytest.mark.parametrize("prec,opt", [(sdg.PREC_FP64, sdg.OPT_OPT1),
+                                      (sdg.PREC_FP64_EMU, sdg.OPT_OPT1),
+                                      (sdg.PREC_FP64, sdg.OPT_EVENODD)])
+def test_full_size_mass_conservation_and_shift_invariance(full_case, prec, opt):
     f = full_case
     N, p, Np = f["N"], f["p"], (f["p"] + 1) ** 3
-    s = sdg.Solver(N, N, N, p, f["D"], f["L"], precision=prec)
+    s = sdg.Solver(N, N, N, p, f["D"], f["L"], opt=opt, precision=prec)
     s.upload(f["q"], f["u"], f["v"], f["w"])
     m0 = W.mass(f["q"], f["x"], N, N, N)
     s.step(f["dt"], 5)
@@ -420,7 +469,7 @@ def test_full_size_mass_conservation_and_shift_invariance(full_case, prec):
     # shifting every input by one element along x shifts the result exactly
     def shift(a):
         return np.roll(a.reshape(N, N, N, Np), 1, axis=2).reshape(-1)
-    s2 = sdg.Solver(N, N, N, p, f["D"], f["L"], precision=prec)
+    s2 = sdg.Solver(N, N, N, p, f["D"], f["L"], opt=opt, precision=prec)
     s2.upload(shift(f["q"]), shift(f["u"]), shift(f["v"]), shift(f["w"]))
     s2.step(f["dt"], 5)
     assert np.array_equal(s2.download(), shift(q))
