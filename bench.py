@@ -318,6 +318,8 @@ def bench_ensemble(sdg, args):
     t0 = time.perf_counter()
     ens = sdg.Ensemble([m["dims"] for m in members], [m["p"] for m in members],
                        [m["dt"] for m in members], ops)
+    if args.batch_opt == "evenodd":
+        ens.set_opt(OPTS["evenodd"])
     for i, m in enumerate(members):
         ens.init_blob(i, m["centre"], m["sigma"], m["vel"])
     sdg.synchronize()
@@ -404,7 +406,7 @@ def bench_order_sweep(sdg, args):
     return out
 
 
-def bench_serving(sdg, args):
+def bench_serving(sdg, args, rate=None):
     """Poisson arrivals of solves (Ne per axis U{4..32}, p U{2..11}, nstep
     U{10..500}, Gaussian tracer in a constant velocity, FP32 compute / FP64
     state) into the continuous-batching server."""
@@ -422,9 +424,10 @@ def bench_serving(sdg, args):
         reqs.append(dict(NeX=dims[0], NeY=dims[1], NeZ=dims[2], p=p, nstep=nstep, dt=dt,
                          centre=[rng.uniform() for _ in range(3)],
                          sigma=0.05 + 0.15 * rng.uniform(), velocity=vel))
-        t += -math.log(1.0 - rng.uniform()) / args.serve_rate
+        t += -math.log(1.0 - rng.uniform()) / (rate or args.serve_rate)
         arrivals.append(t)
-    srv = sdg.Server(ops, hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)))
+    srv = sdg.Server(ops, hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)),
+                     opt=OPTS[args.batch_opt])
     # warm the batched kernel and the pool
     srv.wait(srv.submit(**reqs[0]))
     srv.reset_stats()
@@ -461,10 +464,10 @@ def bench_serving(sdg, args):
                       for r in reqs[:k])
     plain_solves = len(reqs) / (pt * dofs / sample_dofs)
     return {
-        "workload": f"{args.serve_n} requests, Poisson arrivals at {args.serve_rate} req/s, "
+        "workload": f"{args.serve_n} requests, Poisson arrivals at {rate or args.serve_rate} req/s, "
                     f"Ne per axis U{{4..{args.serve_max_ne}}}, p U{{2..11}}, nstep U{{10..500}}, "
                     "FP32 compute / FP64 state, admission by HBM budget",
-        "offered_rate_req_s": args.serve_rate,
+        "offered_rate_req_s": rate or args.serve_rate,
         "solves_per_s": len(reqs) / span,
         "p50_latency_s": float(np.percentile(lat, 50)),
         "p99_latency_s": float(np.percentile(lat, 99)),
@@ -600,6 +603,9 @@ def run_ours(args, ws, rank, local):
         line["ensemble"] = bench_ensemble(sdg, args)
     if ws == 1 and not args.no_serving:
         line["serving"] = bench_serving(sdg, args)
+        # the same request stream offered faster than the GPU can serve it:
+        # throughput and tail latency of the saturated server
+        line["serving_saturated"] = bench_serving(sdg, args, args.serve_rate_saturated)
     if ws == 1 and not args.no_sweep:
         line["order_sweep"] = bench_order_sweep(sdg, args)
     print(json.dumps(line), flush=True)
@@ -617,7 +623,7 @@ def main() -> int:
     ap.add_argument("--p", type=int, default=7)
     ap.add_argument("--ne", type=int, default=32)
     ap.add_argument("--precision", choices=["fp64", "fp64emu", "fp32"], default="fp64")
-    ap.add_argument("--opt", choices=["general", "opt1", "evenodd"], default="opt1",
+    ap.add_argument("--opt", choices=["general", "opt1", "evenodd"], default="evenodd",
                     help="summation order of the FP64 stage: the reference's GENERAL or "
                          "OPT1 order, or the even-odd factorised body")
     ap.add_argument("--seed", type=int, default=20261203)
@@ -628,6 +634,8 @@ def main() -> int:
     ap.add_argument("--no-emu", action="store_true",
                     help="skip the emulated-FP64 measurement beside the FP64 headline")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--batch-opt", choices=["general", "evenodd"], default="general",
+                    help="stage body of the batched kernel (ensemble and serving)")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--sweep-steps", type=int, default=100)
     ap.add_argument("--no-serving", action="store_true")
@@ -635,6 +643,7 @@ def main() -> int:
     ap.add_argument("--ens-steps", type=int, default=100)
     ap.add_argument("--serve-n", type=int, default=60)
     ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-rate-saturated", type=float, default=200.0)
     ap.add_argument("--serve-max-ne", type=int, default=32)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     ap.add_argument("--serve-plain-sample", type=int, default=8)

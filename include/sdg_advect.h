@@ -51,10 +51,11 @@ extern "C" {
 /* DGOptrKernel optimisation types (mod_dg_optr_kernel.f90:38-42). */
 #define SDG_OPT_GENERAL 1
 #define SDG_OPT_OPT1 2
-/* Solver only: the FP64 stage with the even-odd factorisation of D1D and of
- * the face lift (needs their centro-symmetry, which GLL operators have to
- * rounding); ~30 % fewer FP64 operations, same result to rounding.  The
- * FP32 and emulated forms run their OPT1 order for it. */
+/* Solver and batched forms only: the stage with the even-odd factorisation
+ * of D1D and of the face lift (needs their centro-symmetry, which GLL
+ * operators have to rounding); ~30 % fewer FP64 operations in the FP64 form
+ * and far fewer shared-memory reads in the FP32 form, same result to
+ * rounding.  The emulated form runs its own body for every opt type. */
 #define SDG_OPT_EVENODD 3
 
 /* Arithmetic of a solver (the reference is FP64 throughout). */
@@ -278,7 +279,7 @@ typedef struct sdg_solver sdg_solver;
 /* D1D(Nq,Nq) and Lift_mat(Nq,Nq,Nq,6) as read from operator_data (or from
  * sdg_operator_generate).  opt = SDG_OPT_GENERAL / SDG_OPT_OPT1 selects the
  * summation order of the divergence (they differ only for p > 7);
- * SDG_OPT_EVENODD the even-odd FP64 stage (returns SDG_ERR_INVALID_ARG if
+ * SDG_OPT_EVENODD the even-odd stage (returns SDG_ERR_INVALID_ARG if
  * D1D or Lift_mat lacks the centro-symmetry beyond 1e-13 relative).
  * precision = SDG_PREC_*.  stream may be NULL. */
 int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
@@ -367,6 +368,10 @@ int sdg_ensemble_init_blob(sdg_ensemble* e, int i, const double* centre,
  * size by timing stage launches on this ensemble; leaves the state as is. */
 int sdg_ensemble_tune(sdg_ensemble* e);
 int sdg_ensemble_set_epb(sdg_ensemble* e, int p, int epb);
+/* Stage body of the batched kernel: SDG_OPT_GENERAL / SDG_OPT_OPT1 (the
+ * default) the node body with running sums; SDG_OPT_EVENODD the even-odd body
+ * for every order whose operators have the centro-symmetry. */
+int sdg_ensemble_set_opt(sdg_ensemble* e, int opt);
 int sdg_ensemble_set_threads(sdg_ensemble* e, int threads);
 /* epb_by_order receives 12 entries (index = order). */
 int sdg_ensemble_get_config(const sdg_ensemble* e, int* epb_by_order,
@@ -397,6 +402,9 @@ typedef struct {
   int max_window_steps;     /* steps between admission points (default 8) */
   int threads;              /* block size of the batched kernel (0: 256) */
   int epb_by_order[16];     /* elements per block by order (0: default) */
+  int opt;                  /* stage body: 0, SDG_OPT_GENERAL or SDG_OPT_OPT1 =
+                               node body (running sums); SDG_OPT_EVENODD =
+                               even-odd where the operators allow it */
 } sdg_server_config;
 typedef struct {
   int NeX, NeY, NeZ, p, nstep;

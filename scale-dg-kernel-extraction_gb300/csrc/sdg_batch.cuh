@@ -11,7 +11,7 @@
 // stage 3, so one captured CUDA graph replays every step.
 #pragma once
 
-#include "sdg_stage.cuh"
+#include "sdg_stage_eo.cuh"
 
 namespace sdg {
 
@@ -25,10 +25,14 @@ struct BatchInst {
   const float* w;
   const float* D;      // FP32 D1D(Nq,Nq) of this order
   const float* Lift;   // FP32 Lift_mat of this order
+  const float* eo_tab; // FP32 even-odd tables of this order (or null)
   Box box;
   double dt;
   float cdt[3];        // FP32 b_s*dt of the three stages, made on the host
+  float eo_sD[3][3];   // even-odd table factors per stage and direction:
+  float eo_sL[3][3];   // -b_s*dt*Es_d and -b_s*dt*Fs_d/4
   int p;
+  int eo;              // 1: the even-odd body, 0: the node body
   int cur;             // buffer holding the current state
   int active;          // 0: skipped by the stage kernel and by the advance
 };
@@ -42,19 +46,36 @@ struct BatchItem {
 // FP32 increment factors b_s*dt of the three SSP-RK3 stages (mod_common.f90:30).
 inline void batch_stage_factors(BatchInst& I) {
   const double b[3] = {1.0, 0.25, 2.0 / 3.0};
-  for (int s = 0; s < 3; s++) I.cdt[s] = (float)(b[s] * I.dt);
+  for (int s = 0; s < 3; s++) {
+    I.cdt[s] = (float)(b[s] * I.dt);
+    const double c = b[s] * I.dt;
+    for (int d = 0; d < 3; d++) {
+      I.eo_sD[s][d] = (float)(-c * I.box.Es[d]);
+      I.eo_sL[s][d] = (float)(-c * (0.25 * I.box.Fs[d]));
+    }
+  }
 }
 
 // Launches one stage over `n_items` items; counter must be zero on entry.
+// mode: 0 all instances run the node body, 1 all the even-odd body, 2 mixed
+// (batch_mode below).
 int batch_stage_launch(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,
-                       int* d_counter, int grid, int threads, size_t smem, cudaStream_t st);
+                       int* d_counter, int grid, int threads, size_t smem, int mode,
+                       cudaStream_t st);
+template <typename It, typename Get>
+inline int batch_mode(It begin, It end, Get eo_of) {
+  bool any_eo = false, any_node = false;
+  for (It i = begin; i != end; ++i) (eo_of(*i) ? any_eo : any_node) = true;
+  return any_eo ? (any_node ? 2 : 1) : 0;
+}
 // cur = (cur + 1) % 3 for every active instance.
 int batch_advance_launch(BatchInst* d_inst, int n_inst, cudaStream_t st);
-// Dynamic shared memory the kernel needs for `epb` elements of order p.
-size_t batch_smem_bytes(int p, int epb);
+// Dynamic shared memory the kernel needs for `epb` elements of order p with
+// the node body (eo = 0) or the even-odd body (eo = 1).
+size_t batch_smem_bytes(int p, int epb, int eo);
 // Resident blocks of the batch kernel per SM for a block size and smem size.
-int batch_blocks_per_sm(int threads, size_t smem);
-int batch_set_max_smem(size_t smem);
+int batch_blocks_per_sm(int threads, size_t smem, int mode);
+int batch_set_max_smem(size_t smem, int mode);
 
 // Device-side initial condition: Gaussian tracer exp(-d^2/(2 sigma^2)) around
 // `centre` (periodic minimum image on the unit box) and a constant velocity,

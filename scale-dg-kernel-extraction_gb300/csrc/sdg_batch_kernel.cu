@@ -9,12 +9,19 @@ namespace {
 __constant__ double c_rk_a[3] = {0.0, 0.75, 1.0 / 3.0};
 __constant__ double c_rk_b[3] = {1.0, 0.25, 2.0 / 3.0};
 
-template <int P>
-__device__ __forceinline__ void run_order(const StageArgs& a, const BatchItem& w,
+// MODE 0: every instance runs the node body; 1: every instance the even-odd
+// body; 2: either, per instance.  Separate instantiations keep each body's
+// register budget (the combined one needs the larger of the two).
+template <int P, int MODE>
+__device__ __forceinline__ void run_order(const StageArgs& a, const BatchItem& w, int eo,
                                           unsigned char* smem) {
-  stage_block<P, float, float, false>(a, w.e_begin, w.e_count, smem);
+  if (MODE == 1 || (MODE == 2 && eo))
+    stage_eo_block<P, float>(a, w.e_begin, w.e_count, smem);
+  else
+    stage_block<P, float, float, false>(a, w.e_begin, w.e_count, smem);
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(kBatchThreadsMax)
     batch_stage_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
                        int n_items, int stage, int* counter) {
@@ -49,18 +56,26 @@ __global__ void __launch_bounds__(kBatchThreadsMax)
       a.b_is_one = (stage == 0);
       a.a_nonzero = (stage != 0);
       a.tend_only = 0;
+      const int eo = (MODE == 1) ? 1 : (MODE == 0) ? 0 : I.eo;
+      if (eo) {
+        a.D = I.eo_tab;
+        for (int d = 0; d < 3; d++) {
+          a.eo_sDf[d] = I.eo_sD[stage][d];
+          a.eo_sLf[d] = I.eo_sL[stage][d];
+        }
+      }
       switch (I.p) {
-        case 1: run_order<1>(a, w, smem); break;
-        case 2: run_order<2>(a, w, smem); break;
-        case 3: run_order<3>(a, w, smem); break;
-        case 4: run_order<4>(a, w, smem); break;
-        case 5: run_order<5>(a, w, smem); break;
-        case 6: run_order<6>(a, w, smem); break;
-        case 7: run_order<7>(a, w, smem); break;
-        case 8: run_order<8>(a, w, smem); break;
-        case 9: run_order<9>(a, w, smem); break;
-        case 10: run_order<10>(a, w, smem); break;
-        case 11: run_order<11>(a, w, smem); break;
+        case 1: run_order<1, MODE>(a, w, eo, smem); break;
+        case 2: run_order<2, MODE>(a, w, eo, smem); break;
+        case 3: run_order<3, MODE>(a, w, eo, smem); break;
+        case 4: run_order<4, MODE>(a, w, eo, smem); break;
+        case 5: run_order<5, MODE>(a, w, eo, smem); break;
+        case 6: run_order<6, MODE>(a, w, eo, smem); break;
+        case 7: run_order<7, MODE>(a, w, eo, smem); break;
+        case 8: run_order<8, MODE>(a, w, eo, smem); break;
+        case 9: run_order<9, MODE>(a, w, eo, smem); break;
+        case 10: run_order<10, MODE>(a, w, eo, smem); break;
+        case 11: run_order<11, MODE>(a, w, eo, smem); break;
         default: break;
       }
     }
@@ -103,40 +118,53 @@ __global__ void init_blob_kernel(double* q, float* u, float* v, float* w, const 
 }
 
 template <int P>
-size_t smem_for(int epb) {
-  return stage_block_smem<P, float>(epb);
+size_t smem_for(int epb, int eo) {
+  return eo ? eo_block_smem<P, float>(epb) : stage_block_smem<P, float>(epb);
 }
 
 }  // namespace
 
-size_t batch_smem_bytes(int p, int epb) {
+size_t batch_smem_bytes(int p, int epb, int eo) {
   switch (p) {
-    case 1: return smem_for<1>(epb);
-    case 2: return smem_for<2>(epb);
-    case 3: return smem_for<3>(epb);
-    case 4: return smem_for<4>(epb);
-    case 5: return smem_for<5>(epb);
-    case 6: return smem_for<6>(epb);
-    case 7: return smem_for<7>(epb);
-    case 8: return smem_for<8>(epb);
-    case 9: return smem_for<9>(epb);
-    case 10: return smem_for<10>(epb);
-    case 11: return smem_for<11>(epb);
+    case 1: return smem_for<1>(epb, eo);
+    case 2: return smem_for<2>(epb, eo);
+    case 3: return smem_for<3>(epb, eo);
+    case 4: return smem_for<4>(epb, eo);
+    case 5: return smem_for<5>(epb, eo);
+    case 6: return smem_for<6>(epb, eo);
+    case 7: return smem_for<7>(epb, eo);
+    case 8: return smem_for<8>(epb, eo);
+    case 9: return smem_for<9>(epb, eo);
+    case 10: return smem_for<10>(epb, eo);
+    case 11: return smem_for<11>(epb, eo);
     default: return 0;
   }
 }
 
-int batch_set_max_smem(size_t smem) {
-  SDG_CUDA_TRY(cudaFuncSetAttribute(batch_stage_kernel,
+namespace {
+template <int MODE>
+int set_max_smem_mode(size_t smem) {
+  SDG_CUDA_TRY(cudaFuncSetAttribute(batch_stage_kernel<MODE>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   return SDG_OK;
 }
+}  // namespace
 
-int batch_blocks_per_sm(int threads, size_t smem) {
+int batch_set_max_smem(size_t smem, int mode) {
+  if (mode == 1) return set_max_smem_mode<1>(smem);
+  if (mode == 2) return set_max_smem_mode<2>(smem);
+  return set_max_smem_mode<0>(smem);
+}
+
+int batch_blocks_per_sm(int threads, size_t smem, int mode) {
   int nb = 0;
-  if (batch_set_max_smem(smem) != SDG_OK) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel, threads, smem) !=
-      cudaSuccess) {
+  if (batch_set_max_smem(smem, mode) != SDG_OK) return 0;
+  cudaError_t ce = (mode == 1)
+      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<1>, threads, smem)
+      : (mode == 2)
+      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<2>, threads, smem)
+      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<0>, threads, smem);
+  if (ce != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -144,9 +172,15 @@ int batch_blocks_per_sm(int threads, size_t smem) {
 }
 
 int batch_stage_launch(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,
-                       int* d_counter, int grid, int threads, size_t smem, cudaStream_t st) {
+                       int* d_counter, int grid, int threads, size_t smem, int mode,
+                       cudaStream_t st) {
   if (n_items <= 0) return SDG_OK;
-  batch_stage_kernel<<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage, d_counter);
+  if (mode == 1)
+    batch_stage_kernel<1><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage, d_counter);
+  else if (mode == 2)
+    batch_stage_kernel<2><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage, d_counter);
+  else
+    batch_stage_kernel<0><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage, d_counter);
   SDG_CUDA_TRY(cudaGetLastError());
   return SDG_OK;
 }

@@ -22,12 +22,14 @@ struct sdg_ensemble {
   int n_items = 0;
   int* d_counter = nullptr;        // 3 stage counters
   void* arena = nullptr;
-  float* d_ops[kBatchMaxOrder + 1][2] = {};
+  float* d_ops[kBatchMaxOrder + 1][3] = {};  // D1D, Lift, even-odd tables (FP32)
+  bool use_eo = false;             // even-odd body (where the operators allow it)
   double* d_x1D[kBatchMaxOrder + 1] = {};
   int epb[kBatchMaxOrder + 1] = {};
   int threads = 256;
   size_t smem = 0;
   int grid = 0;
+  int mode = 0;                    // batch kernel body mode (batch_mode)
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   long long total_dof = 0;
@@ -51,6 +53,7 @@ void free_ensemble(sdg_ensemble* e) {
   for (int p = 0; p <= kBatchMaxOrder; p++) {
     cudaFree(e->d_ops[p][0]);
     cudaFree(e->d_ops[p][1]);
+    cudaFree(e->d_ops[p][2]);
     cudaFree(e->d_x1D[p]);
   }
 }
@@ -71,7 +74,7 @@ int build_items(sdg_ensemble* e, const std::vector<int>* subset = nullptr) {
     const int epb = e->epb[I.p];
     for (long long b = 0; b < I.box.Ne; b += epb)
       items.push_back({i, (int)b, (int)std::min<long long>(epb, I.box.Ne - b)});
-    smem = std::max(smem, batch_smem_bytes(I.p, epb));
+    smem = std::max(smem, batch_smem_bytes(I.p, epb, I.eo));
   }
   cudaFree(e->d_items);
   e->d_items = nullptr;
@@ -82,10 +85,11 @@ int build_items(sdg_ensemble* e, const std::vector<int>* subset = nullptr) {
                             cudaMemcpyHostToDevice));
   }
   e->smem = smem;
+  e->mode = batch_mode(idx.begin(), idx.end(), [&](int i) { return e->inst[i].eo != 0; });
   int dev = 0, nsm = 0;
   SDG_CUDA_TRY(cudaGetDevice(&dev));
   SDG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const int per_sm = batch_blocks_per_sm(e->threads, smem);
+  const int per_sm = batch_blocks_per_sm(e->threads, smem, e->mode);
   if (per_sm <= 0)
     return fail(SDG_ERR_INVALID_ARG, "batch kernel does not fit: %d threads, %zu B smem",
                 e->threads, smem);
@@ -97,7 +101,7 @@ int enqueue_step(sdg_ensemble* e) {
   SDG_CUDA_TRY(cudaMemsetAsync(e->d_counter, 0, 3 * sizeof(int), e->stream));
   for (int s = 0; s < 3; s++)
     SDG_TRY(batch_stage_launch(e->d_inst, e->d_items, e->n_items, s, e->d_counter + s, e->grid,
-                               e->threads, e->smem, e->stream));
+                               e->threads, e->smem, e->mode, e->stream));
   return batch_advance_launch(e->d_inst, e->n, e->stream);
 }
 
@@ -139,7 +143,7 @@ int time_stage0(sdg_ensemble* e, float* ms) {
     SDG_CUDA_TRY(cudaMemsetAsync(e->d_counter, 0, sizeof(int), e->stream));
     SDG_CUDA_TRY(cudaEventRecord(a, e->stream));
     SDG_TRY(batch_stage_launch(e->d_inst, e->d_items, e->n_items, 0, e->d_counter, e->grid,
-                               e->threads, e->smem, e->stream));
+                               e->threads, e->smem, e->mode, e->stream));
     SDG_CUDA_TRY(cudaEventRecord(b, e->stream));
     SDG_CUDA_TRY(cudaEventSynchronize(b));
     float t = 0.f;
@@ -202,6 +206,14 @@ int sdg_ensemble_create(sdg_ensemble** out, int n, const int* dims, const int* o
       ce = cudaMalloc(&e->d_x1D[p], 8 * nq);
       if (ce == cudaSuccess) ce = cudaMemcpy(e->d_x1D[p], x1D_by_order[p], 8 * nq, cudaMemcpyHostToDevice);
     }
+    // even-odd tables when the operators have the centro-symmetry
+    std::vector<double> eo;
+    if (ce == cudaSuccess && eo_tables(nq, D1D_by_order[p], Lift_by_order[p], eo) == SDG_OK) {
+      std::vector<float> ef(eo.begin(), eo.end());
+      ce = cudaMalloc(&e->d_ops[p][2], 4 * ef.size());
+      if (ce == cudaSuccess)
+        ce = cudaMemcpy(e->d_ops[p][2], ef.data(), 4 * ef.size(), cudaMemcpyHostToDevice);
+    }
     if (ce != cudaSuccess) return bail(cuda_fail(ce, "ensemble operators", __FILE__, __LINE__));
   }
   // one arena: per instance 3 FP64 state buffers and 3 FP32 velocity arrays
@@ -230,6 +242,8 @@ int sdg_ensemble_create(sdg_ensemble** out, int n, const int* dims, const int* o
     I.w = vel + 2 * nd;
     I.D = e->d_ops[p][0];
     I.Lift = e->d_ops[p][1];
+    I.eo_tab = e->d_ops[p][2];
+    I.eo = (I.eo_tab != nullptr && e->use_eo) ? 1 : 0;
     I.dt = dt[i];
     batch_stage_factors(I);
     I.p = p;
@@ -296,6 +310,29 @@ int sdg_ensemble_set_threads(sdg_ensemble* e, int threads) {
   return build_items(e);
 }
 
+int sdg_ensemble_set_opt(sdg_ensemble* e, int opt) {
+  if (!e) return fail(SDG_ERR_INVALID_ARG, "NULL ensemble");
+  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1 && opt != SDG_OPT_EVENODD)
+    return fail(SDG_ERR_BAD_OPTTYPE, "unknown opt type %d", opt);
+  e->use_eo = (opt == SDG_OPT_EVENODD);
+  // the device copy holds the live buffer indices: update only the body flag
+  SDG_CUDA_TRY(cudaStreamSynchronize(e->stream));
+  std::vector<BatchInst> live(e->n);
+  SDG_CUDA_TRY(cudaMemcpy(live.data(), e->d_inst, sizeof(BatchInst) * e->n,
+                          cudaMemcpyDeviceToHost));
+  for (int i = 0; i < e->n; i++) {
+    e->inst[i].eo = (e->inst[i].eo_tab != nullptr && e->use_eo) ? 1 : 0;
+    live[i].eo = e->inst[i].eo;
+  }
+  SDG_CUDA_TRY(cudaMemcpy(e->d_inst, live.data(), sizeof(BatchInst) * e->n,
+                          cudaMemcpyHostToDevice));
+  if (e->graph) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  return build_items(e);
+}
+
 int sdg_ensemble_get_config(const sdg_ensemble* e, int* epb_by_order, int* threads, int* grid) {
   if (!e) return fail(SDG_ERR_INVALID_ARG, "NULL ensemble");
   if (epb_by_order)
@@ -334,7 +371,7 @@ int sdg_ensemble_tune(sdg_ensemble* e) {
       float best = 1e30f;
       for (int cand = 1; cand <= 256; cand *= 2) {
         if (cand * np > 4096 || (cand * np < 64 && cand * 2 * np <= 4096)) continue;
-        if (batch_smem_bytes(p, cand) > 96 * 1024) continue;
+        if (batch_smem_bytes(p, cand, e->inst[by_order[p][0]].eo) > 96 * 1024) continue;
         e->epb[p] = cand;
         if (build_items(e, &by_order[p]) != SDG_OK) continue;
         float ms = 0.f;

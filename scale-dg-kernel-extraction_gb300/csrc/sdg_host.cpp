@@ -161,6 +161,80 @@ void gll_nodes(int N, long double* x) {
 }
 }  // namespace
 
+// Tables of the even-odd stage bodies (sdg_stage_eo.cuh), per direction x, y,
+// z: E(i,l), O(i,l), D(i,mid) from the centro-antisymmetric part of D1D and
+// A(i), B(i) from the face lift columns.  Checks, relative to max|D| and
+// max|Lift|, that D1D is centro-antisymmetric, that each face's lift is a
+// column along the normal constant over the tangential nodes and that the +
+// face's column mirrors the - face's, all within 1e-13 (the operator files
+// hold them to 2.4e-14 at p = 15), then builds the tables from the
+// symmetrised operators in long double.
+int eo_tables(int Nq, const double* D1D, const double* Lift_mat, std::vector<double>& tab) {
+  const int N = Nq, H = N / 2, HR = (N + 1) / 2, ODD = N & 1;
+  const int TE = H * H + HR * H + ODD * H + HR + H;
+  const long long Np = (long long)N * N * N;
+  const double tol = 1e-13;
+  double maxD = 0.0, maxL = 0.0;
+  for (int i = 0; i < N * N; i++) maxD = std::fmax(maxD, std::fabs(D1D[i]));
+  for (long long i = 0; i < 6 * Np; i++) maxL = std::fmax(maxL, std::fabs(Lift_mat[i]));
+  auto D = [&](int i, int l) { return (long double)D1D[i + l * N]; };
+  for (int i = 0; i < N; i++)
+    for (int l = 0; l < N; l++)
+      if (std::fabs(D1D[i + l * N] + D1D[(N - 1 - i) + (N - 1 - l) * N]) > tol * maxD)
+        return fail(SDG_ERR_INVALID_ARG,
+                    "D1D is not centro-antisymmetric (entry %d,%d); use SDG_OPT_OPT1", i, l);
+  // lift column of face f along its normal: mean over the tangential nodes
+  const int fminus[3] = {3, 0, 4}, fplus[3] = {1, 2, 5};
+  auto node = [&](int ax, int m, int t1, int t2) {
+    // normal index m on axis ax, tangential indices on the other two axes
+    int c[3];
+    c[ax] = m;
+    c[(ax + 1) % 3] = t1;
+    c[(ax + 2) % 3] = t2;
+    return c[0] + (long long)c[1] * N + (long long)c[2] * N * N;
+  };
+  std::vector<long double> col(2 * (size_t)N);
+  tab.assign(3 * (size_t)TE, 0.0);
+  for (int ax = 0; ax < 3; ax++) {
+    for (int side = 0; side < 2; side++) {
+      const int f = side ? fplus[ax] : fminus[ax];
+      for (int m = 0; m < N; m++) {
+        long double sum = 0.0L;
+        for (int t1 = 0; t1 < N; t1++)
+          for (int t2 = 0; t2 < N; t2++) sum += Lift_mat[node(ax, m, t1, t2) + f * Np];
+        const long double mean = sum / ((long double)N * N);
+        for (int t1 = 0; t1 < N; t1++)
+          for (int t2 = 0; t2 < N; t2++)
+            if (std::fabs((double)(Lift_mat[node(ax, m, t1, t2) + f * Np] - mean)) > tol * maxL)
+              return fail(SDG_ERR_INVALID_ARG,
+                          "Lift_mat face %d is not separable; use SDG_OPT_OPT1", f + 1);
+        col[side * N + m] = mean;
+      }
+    }
+    for (int m = 0; m < N; m++)
+      if (std::fabs((double)(col[m] - col[N + (N - 1 - m)])) > tol * maxL)
+        return fail(SDG_ERR_INVALID_ARG,
+                    "Lift_mat faces %d/%d are not mirror images; use SDG_OPT_OPT1",
+                    fminus[ax] + 1, fplus[ax] + 1);
+    double* T = tab.data() + (size_t)ax * TE;
+    auto Ds = [&](int i, int l) { return 0.5L * (D(i, l) - D(N - 1 - i, N - 1 - l)); };
+    for (int i = 0; i < H; i++)
+      for (int l = 0; l < H; l++) T[i * H + l] = (double)(0.5L * (Ds(i, l) + Ds(i, N - 1 - l)));
+    for (int i = 0; i < HR; i++)
+      for (int l = 0; l < H; l++)
+        T[H * H + i * H + l] = (double)(0.5L * (Ds(i, l) - Ds(i, N - 1 - l)));
+    if (ODD)
+      for (int i = 0; i < H; i++) T[H * H + HR * H + i] = (double)Ds(i, H);
+    // symmetrised minus-face column lam(m); the plus face is lam(N-1-m)
+    auto lam = [&](int m) { return 0.5L * (col[m] + col[N + (N - 1 - m)]); };
+    const int oA = H * H + HR * H + ODD * H, oB = oA + HR;
+    for (int i = 0; i < HR; i++) T[oA + i] = (double)(0.5L * (lam(i) + lam(N - 1 - i)));
+    for (int i = 0; i < H; i++) T[oB + i] = (double)(0.5L * (lam(i) - lam(N - 1 - i)));
+  }
+  return SDG_OK;
+}
+
+
 }  // namespace sdg
 
 using namespace sdg;

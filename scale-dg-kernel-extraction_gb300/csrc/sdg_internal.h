@@ -5,6 +5,7 @@
 
 #include <cstdarg>
 #include <cstdint>
+#include <vector>
 
 #include "sdg_advect.h"
 
@@ -71,7 +72,12 @@ struct StageArgs {
   // of the lift part (-c*Fs_d/4) of the tables, c = b*dt (1 for tend_only);
   // D then points at the 3-direction table built by the solver
   double eo_sD[3], eo_sL[3];
+  float eo_sDf[3], eo_sLf[3];  // the same factors for the FP32-compute form
 };
+
+// Even-odd tables (3 directions, unscaled) from D1D and Lift_mat after the
+// symmetry checks; SDG_ERR_INVALID_ARG when the operators lack them.
+int eo_tables(int Nq, const double* D1D, const double* Lift_mat, std::vector<double>& tab);
 
 // Fused stage launchers (sdg_stage_*.cu).  prec = SDG_PREC_*.
 int launch_stage(int p, int prec, int opt, const StageArgs& a, cudaStream_t st);

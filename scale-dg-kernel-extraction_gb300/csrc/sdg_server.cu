@@ -49,7 +49,7 @@ struct Req {
 
 struct sdg_server {
   sdg_server_config cfg{};
-  float* d_ops[kBatchMaxOrder + 1][2] = {};
+  float* d_ops[kBatchMaxOrder + 1][3] = {};  // D1D, Lift, even-odd tables (FP32)
   double* d_x1D[kBatchMaxOrder + 1] = {};
   cudaStream_t stream = nullptr;
   cudaMemPool_t pool = nullptr;
@@ -71,6 +71,7 @@ struct sdg_server {
   int* d_counter = nullptr;
   size_t smem = 0;
   int grid = 0;
+  int mode = 0;  // batch kernel body mode of the active set (batch_mode)
   int threads = 256;
   int epb[kBatchMaxOrder + 1] = {};
   // statistics
@@ -111,6 +112,8 @@ int admit(sdg_server* s, Req* q) {
   I.w = vel + 2 * nd;
   I.D = s->d_ops[q->r.p][0];
   I.Lift = s->d_ops[q->r.p][1];
+  I.eo_tab = s->d_ops[q->r.p][2];
+  I.eo = (I.eo_tab != nullptr) ? 1 : 0;
   I.dt = q->r.dt;
   batch_stage_factors(I);
   I.p = q->r.p;
@@ -141,7 +144,7 @@ int rebuild_tables(sdg_server* s) {
     const int e = s->epb[I.p];
     for (long long b = 0; b < I.box.Ne; b += e)
       items.push_back({i, (int)b, (int)std::min<long long>(e, I.box.Ne - b)});
-    smem = std::max(smem, batch_smem_bytes(I.p, e));
+    smem = std::max(smem, batch_smem_bytes(I.p, e, I.eo));
   }
   if (n > s->d_inst_cap) {
     cudaFree(s->d_inst);
@@ -164,12 +167,14 @@ int rebuild_tables(sdg_server* s) {
   // the host vectors must outlive the asynchronous copies
   SDG_CUDA_TRY(cudaStreamSynchronize(s->stream));
   s->n_items = (int)items.size();
-  if (smem > s->smem || s->grid == 0) {
+  const int mode = batch_mode(inst.begin(), inst.end(), [](const BatchInst& I) { return I.eo != 0; });
+  if (smem > s->smem || s->grid == 0 || mode != s->mode) {
     s->smem = std::max(smem, s->smem);
+    s->mode = mode;
     int dev = 0, nsm = 0;
     SDG_CUDA_TRY(cudaGetDevice(&dev));
     SDG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const int per_sm = batch_blocks_per_sm(s->threads, s->smem);
+    const int per_sm = batch_blocks_per_sm(s->threads, s->smem, s->mode);
     if (per_sm <= 0) return fail(SDG_ERR_INVALID_ARG, "batch kernel does not fit");
     s->grid = nsm * per_sm;
   }
@@ -182,7 +187,7 @@ int run_steps(sdg_server* s, int nsteps) {
     SDG_CUDA_TRY(cudaMemsetAsync(s->d_counter, 0, 3 * sizeof(int), s->stream));
     for (int st = 0; st < 3; st++)
       SDG_TRY(batch_stage_launch(s->d_inst, s->d_items, s->n_items, st, s->d_counter + st,
-                                 s->grid, s->threads, s->smem, s->stream));
+                                 s->grid, s->threads, s->smem, s->mode, s->stream));
     SDG_TRY(batch_advance_launch(s->d_inst, n, s->stream));
     s->launches += 4;
   }
@@ -321,6 +326,9 @@ int sdg_server_create(sdg_server** out, const sdg_server_config* cfg,
   *out = nullptr;
   if (cfg->max_active < 1 || cfg->hbm_budget_bytes == 0)
     return fail(SDG_ERR_INVALID_ARG, "server needs at least one slot and a budget");
+  if (cfg->opt != 0 && cfg->opt != SDG_OPT_GENERAL && cfg->opt != SDG_OPT_OPT1 &&
+      cfg->opt != SDG_OPT_EVENODD)
+    return fail(SDG_ERR_BAD_OPTTYPE, "unknown opt type %d", cfg->opt);
   SDG_TRY(require_device());
   sdg_server* s = new (std::nothrow) sdg_server();
   if (!s) return fail(SDG_ERR_OUT_OF_MEMORY, "host allocation failed");
@@ -335,6 +343,7 @@ int sdg_server_create(sdg_server** out, const sdg_server_config* cfg,
     for (int p = 0; p <= kBatchMaxOrder; p++) {
       cudaFree(s->d_ops[p][0]);
       cudaFree(s->d_ops[p][1]);
+      cudaFree(s->d_ops[p][2]);
       cudaFree(s->d_x1D[p]);
     }
     cudaFree(s->d_counter);
@@ -371,6 +380,16 @@ int sdg_server_create(sdg_server** out, const sdg_server_config* cfg,
     if (ce == cudaSuccess) ce = cudaMemcpy(s->d_ops[p][1], l.data(), 4 * nl, cudaMemcpyHostToDevice);
     if (ce == cudaSuccess)
       ce = cudaMemcpy(s->d_x1D[p], x1D_by_order[p], 8 * nq, cudaMemcpyHostToDevice);
+    // even-odd tables (opt EVENODD) when the operators have the symmetry
+    std::vector<double> eo;
+    const bool want_eo = (cfg->opt == SDG_OPT_EVENODD);
+    if (ce == cudaSuccess && want_eo &&
+        eo_tables(nq, D1D_by_order[p], Lift_by_order[p], eo) == SDG_OK) {
+      std::vector<float> ef(eo.begin(), eo.end());
+      ce = cudaMalloc(&s->d_ops[p][2], 4 * ef.size());
+      if (ce == cudaSuccess)
+        ce = cudaMemcpy(s->d_ops[p][2], ef.data(), 4 * ef.size(), cudaMemcpyHostToDevice);
+    }
   }
   if (ce != cudaSuccess) return bail(cuda_fail(ce, "server setup", __FILE__, __LINE__));
   try {
@@ -497,6 +516,7 @@ int sdg_server_destroy(sdg_server* s) {
   for (int p = 0; p <= kBatchMaxOrder; p++) {
     cudaFree(s->d_ops[p][0]);
     cudaFree(s->d_ops[p][1]);
+    cudaFree(s->d_ops[p][2]);
     cudaFree(s->d_x1D[p]);
   }
   cudaFree(s->d_inst);

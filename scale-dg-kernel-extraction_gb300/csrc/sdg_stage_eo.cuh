@@ -1,10 +1,12 @@
-// Fused FP64 RK-stage kernel with the even-odd factorisation of the 1D
-// operators (opt type SDG_OPT_EVENODD).
+// Fused RK-stage kernel with the even-odd factorisation of the 1D operators
+// (opt type SDG_OPT_EVENODD), for the FP64 form and the FP32-compute form.
 //
 // On GB300 the FP64 pipe runs at 1/64 of the FP32 rate, so the plain FP64
 // stage is bound by its count of FP64 instructions, not by HBM.  This body
 // computes the same tendency and stage update as stage_block<P, double> with
-// about 30 % fewer FP64 instructions per node:
+// about 30 % fewer FP64 instructions per node; in FP32 it also replaces the
+// node body's per-node shared-memory reads of a whole line by one read per
+// line value:
 //
 //  * Centro-antisymmetry of the GLL differentiation matrix,
 //    D(N-1-i, N-1-l) = -D(i, l), splits a line's N-term sums into pairs:
@@ -63,47 +65,50 @@ struct EoCfg {
   static constexpr int EPB = (256 / Ord<P>::NQ2) > 0 ? 256 / Ord<P>::NQ2 : 1;
 };
 
-template <int P>
-__host__ __device__ constexpr size_t eo_smem_bytes() {
+// Dynamic shared memory of one block with nloc elements: the three scaled
+// direction tables, then per element q, F_x (later the line-result sums), F_y,
+// F_z and the 6 Nfp face fluxes, then the neighbour indices.
+template <int P, typename CT>
+__host__ __device__ constexpr size_t eo_block_smem(int nloc) {
   using O = Ord<P>;
-  return sizeof(double) *
-             (size_t)(3 * EoShape<P>::TE + EoCfg<P>::EPB * (4 * O::NP + O::NFT)) +
-         sizeof(int) * 6 * EoCfg<P>::EPB;
+  return sizeof(CT) * (size_t)(3 * EoShape<P>::TE + nloc * (4 * O::NP + O::NFT)) +
+         sizeof(int) * 6 * (size_t)nloc;
 }
 
-__device__ __forceinline__ double abs_bits(double x) {
+__device__ __forceinline__ double abs_ct(double x) {
   return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
 }
+__device__ __forceinline__ float abs_ct(float x) { return fabsf(x); }
 
 // One line: F (stride S) holds the line's N volume fluxes, T the direction's
 // scaled tables, gm / gp the face fluxes of the line's - and + faces.  The
 // N results go to emit(m, value) after all reads of F.
-template <int P, int S, typename Emit>
-__device__ __forceinline__ void eo_line(const double* F, const double* __restrict__ T, double gm,
-                                        double gp, Emit&& emit) {
+template <int P, int S, typename CT, typename Emit>
+__device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, CT gm, CT gp,
+                                        Emit&& emit) {
   using Sh = EoShape<P>;
   constexpr int N = Sh::N, H = Sh::H;
-  double s[H], d[H];
+  CT s[H], d[H];
 #pragma unroll
   for (int l = 0; l < H; l++) {
-    const double lo = F[l * S], hi = F[(N - 1 - l) * S];
+    const CT lo = F[l * S], hi = F[(N - 1 - l) * S];
     s[l] = lo + hi;
     d[l] = lo - hi;
   }
-  double fm = 0.0;
+  CT fm = CT(0);
   if constexpr (Sh::ODD != 0) fm = F[H * S];
-  const double gs = gm + gp, gd = gm - gp;
+  const CT gs = gm + gp, gd = gm - gp;
   // rows unrolled up to p = 7; above that a rolled loop keeps the 2H line
   // values and the row sums within the register budget
   constexpr int kRowUnroll = (N <= 8) ? H : 1;
 #pragma unroll kRowUnroll
   for (int i = 0; i < H; i++) {
-    double e = T[Sh::OFF_E + i * H] * s[0];
+    CT e = T[Sh::OFF_E + i * H] * s[0];
 #pragma unroll
     for (int l = 1; l < H; l++) e = fma(T[Sh::OFF_E + i * H + l], s[l], e);
     if constexpr (Sh::ODD != 0) e = fma(T[Sh::OFF_DM + i], fm, e);
     e = fma(T[Sh::OFF_B + i], gd, e);
-    double o = T[Sh::OFF_O + i * H] * d[0];
+    CT o = T[Sh::OFF_O + i * H] * d[0];
 #pragma unroll
     for (int l = 1; l < H; l++) o = fma(T[Sh::OFF_O + i * H + l], d[l], o);
     o = fma(T[Sh::OFF_A + i], gs, o);
@@ -111,7 +116,7 @@ __device__ __forceinline__ void eo_line(const double* F, const double* __restric
     emit(N - 1 - i, o - e);
   }
   if constexpr (Sh::ODD != 0) {
-    double o = T[Sh::OFF_O + H * H] * d[0];
+    CT o = T[Sh::OFF_O + H * H] * d[0];
 #pragma unroll
     for (int l = 1; l < H; l++) o = fma(T[Sh::OFF_O + H * H + l], d[l], o);
     o = fma(T[Sh::OFF_A + H], gs, o);
@@ -119,41 +124,60 @@ __device__ __forceinline__ void eo_line(const double* F, const double* __restric
   }
 }
 
-template <int P>
-__global__ void __launch_bounds__(EoCfg<P>::THREADS) stage_eo_kernel(const StageArgs a) {
+// One block advances elements [eb, eb + nloc) through one stage with the
+// even-odd body.  CT = double: FP64 throughout (tables scaled by eo_sD /
+// eo_sL).  CT = float: the FP32-compute form (FP32 tables, velocity and
+// sums, scaled by eo_sDf / eo_sLf), with the increment widened by bits and
+// the RK combination in FP64.  Block size and nloc are runtime values, so the
+// batched persistent kernel can use the same body.
+template <int P, typename CT>
+__device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb, int nloc,
+                                               unsigned char* smem) {
   using O = Ord<P>;
   using Sh = EoShape<P>;
   constexpr int NQ = O::NQ, NQ2 = O::NQ2, NP = O::NP, NFP = O::NFP, NFT = O::NFT;
-  constexpr int EPB = EoCfg<P>::EPB, T = EoCfg<P>::THREADS, TE = Sh::TE;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* sT = reinterpret_cast<double*>(smem_raw);  // 3 directions x TE
-  const long long eb = a.elem_begin + (long long)blockIdx.x * EPB;
-  const long long eend = a.elem_begin + a.elem_count;
-  const int nloc = (int)((eend - eb) < EPB ? (eend - eb) : EPB);
-  if (nloc <= 0) return;
-  double* sq = sT + 3 * TE;
-  double* sFx = sq + nloc * NP;  // F_x, then the running sum of the line results
-  double* sFy = sFx + nloc * NP;
-  double* sFz = sFy + nloc * NP;
-  double* sf = sFz + nloc * NP;
+  constexpr int TE = Sh::TE;
+  constexpr bool kF64 = sizeof(CT) == 8;
+  const int T = blockDim.x;
+  CT* sT = reinterpret_cast<CT*>(smem);  // 3 directions x TE
+  CT* sq = sT + 3 * TE;
+  CT* sFx = sq + nloc * NP;  // F_x, then the running sum of the line results
+  CT* sFy = sFx + nloc * NP;
+  CT* sFz = sFy + nloc * NP;
+  CT* sf = sFz + nloc * NP;
   int* snb = reinterpret_cast<int*>(sf + nloc * NFT);
 
   const double* __restrict__ qin = a.q_in;
-  const double* __restrict__ gu = static_cast<const double*>(a.u);
-  const double* __restrict__ gv = static_cast<const double*>(a.v);
-  const double* __restrict__ gw = static_cast<const double*>(a.w);
-  const double* __restrict__ tab = static_cast<const double*>(a.D);
+  const CT* __restrict__ gu = static_cast<const CT*>(a.u);
+  const CT* __restrict__ gv = static_cast<const CT*>(a.v);
+  const CT* __restrict__ gw = static_cast<const CT*>(a.w);
+  const CT* __restrict__ tab = static_cast<const CT*>(a.D);
   const long long g0 = eb * NP;
 
-  // phase 0: scaled tables, neighbours, q and F_d = q * u_d
+  // phase 0: scaled tables, neighbours, q and F_d = q * u_d.  The factors
+  // are picked by selects, not by a runtime array index, so that the
+  // argument struct can stay in registers in the batched kernel.
+  CT fD[3], fL[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if constexpr (kF64) {
+      fD[d] = a.eo_sD[d];
+      fL[d] = a.eo_sL[d];
+    } else {
+      fD[d] = a.eo_sDf[d];
+      fL[d] = a.eo_sLf[d];
+    }
+  }
   for (int t = threadIdx.x; t < 3 * TE; t += T) {
     const int dir = t / TE, w = t - dir * TE;
-    sT[t] = tab[t] * (w < Sh::OFF_A ? a.eo_sD[dir] : a.eo_sL[dir]);
+    const CT sd = (dir == 0) ? fD[0] : (dir == 1) ? fD[1] : fD[2];
+    const CT sl = (dir == 0) ? fL[0] : (dir == 1) ? fL[1] : fL[2];
+    sT[t] = tab[t] * ((w < Sh::OFF_A) ? sd : sl);
   }
   for (int t = threadIdx.x; t < 6 * nloc; t += T)
     snb[t] = (int)neighbor(a.box, eb + t / 6, t % 6);
   for (int t = threadIdx.x; t < nloc * NP; t += T) {
-    const double qq = qin[g0 + t];
+    const CT qq = to_ct<CT>(qin[g0 + t]);
     sq[t] = qq;
     sFx[t] = qq * gu[g0 + t];
     sFy[t] = qq * gv[g0 + t];
@@ -171,14 +195,14 @@ __global__ void __launch_bounds__(EoCfg<P>::THREADS) stage_eo_kernel(const Stage
     face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sg);
     const long long gM = g0 + (long long)le * NP + nM;
     const long long gP = (long long)snb[6 * le + f] * NP + nP;
-    const double* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
-    const double uM = gvel[gM], uP = gvel[gP];
-    const double qM = sq[le * NP + nM];
-    const double qP = qin[gP];
-    const double a2 = abs_bits(uP + uM);
-    const double tw = (sg > 0) ? 2.0 : -2.0;
-    const double tP = fma(tw, uP, -a2);
-    const double tM = fma(tw, uM, -a2);
+    const CT* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
+    const CT uM = gvel[gM], uP = gvel[gP];
+    const CT qM = sq[le * NP + nM];
+    const CT qP = to_ct<CT>(qin[gP]);
+    const CT a2 = abs_ct(uP + uM);
+    const CT tw = (sg > 0) ? CT(2) : CT(-2);
+    const CT tP = fma(tw, uP, -a2);
+    const CT tM = fma(tw, uM, -a2);
     sf[le * NFT + r] = fma(qP, tP, -(qM * tM));
   }
   __syncthreads();
@@ -186,9 +210,9 @@ __global__ void __launch_bounds__(EoCfg<P>::THREADS) stage_eo_kernel(const Stage
   // phase 2x: lines along i, faces -x (3) and +x (1); results over F_x
   for (int t = threadIdx.x; t < nloc * NQ2; t += T) {
     const int le = t / NQ2, r = t - le * NQ2;
-    double* F = sFx + le * NP + r * NQ;
-    const double* fl = sf + le * NFT + r;
-    eo_line<P, 1>(F, sT, fl[3 * NFP], fl[1 * NFP], [&](int m, double v) { F[m] = v; });
+    CT* F = sFx + le * NP + r * NQ;
+    const CT* fl = sf + le * NFT + r;
+    eo_line<P, 1>(F, sT, fl[3 * NFP], fl[1 * NFP], [&](int m, CT v) { F[m] = v; });
   }
   __syncthreads();
 
@@ -196,48 +220,78 @@ __global__ void __launch_bounds__(EoCfg<P>::THREADS) stage_eo_kernel(const Stage
   for (int t = threadIdx.x; t < nloc * NQ2; t += T) {
     const int le = t / NQ2, r = t - le * NQ2;
     const int off = le * NP + (r % NQ) + (r / NQ) * NQ2;
-    double* acc = sFx + off;
-    const double* fl = sf + le * NFT + r;
+    CT* acc = sFx + off;
+    const CT* fl = sf + le * NFT + r;
     eo_line<P, NQ>(sFy + off, sT + TE, fl[0], fl[2 * NFP],
-                   [&](int m, double v) { acc[m * NQ] += v; });
+                   [&](int m, CT v) { acc[m * NQ] += v; });
   }
   __syncthreads();
 
   // phase 2z: lines along k, faces -z (4) and +z (5); finish the node and the
-  // RK update q_out = b*q + inc (+ a*q0)
+  // RK update q_out = b*q + inc (+ a*q0).  The lambda captures plain locals,
+  // not the argument struct, which would otherwise live in local memory when
+  // the batched kernel builds it per work item.
+  double* __restrict__ qout = a.q_out;
+  const double* __restrict__ q0 = a.q0;
+  const double rk_a = a.a, rk_b = a.b;
+  const int tend_only = a.tend_only, b_is_one = a.b_is_one, a_nonzero = a.a_nonzero;
   for (int t = threadIdx.x; t < nloc * NQ2; t += T) {
     const int le = t / NQ2, r = t - le * NQ2;
     const int off = le * NP + r;
-    const double* fl = sf + le * NFT + r;
-    eo_line<P, NQ2>(sFz + off, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], [&](int m, double v) {
+    const CT* fl = sf + le * NFT + r;
+    eo_line<P, NQ2>(sFz + off, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], [&](int m, CT v) {
       const int n = off + m * NQ2;
-      const double inc = sFx[n] + v;
       const long long g = g0 + n;
-      if (a.tend_only) {
-        a.q_out[g] = inc;
+      double inc, qv = 0.0;
+      if constexpr (kF64) {
+        inc = sFx[n] + v;
+        qv = sq[n];
       } else {
-        const double qv = sq[n];
-        double res = a.b_is_one ? qv + inc : fma(a.b, qv, inc);
-        if (a.a_nonzero) res = fma(a.a, a.q0[g], res);
-        a.q_out[g] = res;
+        inc = f32_to_f64_bits(sFx[n] + v);
+      }
+      if (tend_only) {
+        qout[g] = inc;
+      } else {
+        if constexpr (!kF64) qv = qin[g];
+        double res = b_is_one ? qv + inc : fma(rk_b, qv, inc);
+        if (a_nonzero) res = fma(rk_a, q0[g], res);
+        qout[g] = res;
       }
     });
   }
 }
 
-template <int P>
+// FP32: at least 4 resident blocks of 256 (registers capped at 64), since
+// the FP32 body issues few instructions per byte and needs the warps to hide
+// memory latency; FP64 is bound by the FP64 pipe and keeps its registers.
+template <int P, typename CT>
+__global__ void __launch_bounds__(EoCfg<P>::THREADS, sizeof(CT) == 4 ? 4 : 1)
+    stage_eo_kernel(const StageArgs a) {
+  constexpr int EPB = EoCfg<P>::EPB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const long long eb = a.elem_begin + (long long)blockIdx.x * EPB;
+  const long long eend = a.elem_begin + a.elem_count;
+  const int nloc = (int)((eend - eb) < EPB ? (eend - eb) : EPB);
+  if (nloc <= 0) return;
+  stage_eo_block<P, CT>(a, eb, nloc, smem_raw);
+}
+
+template <int P, typename CT>
 int launch_stage_eo_impl(const StageArgs& a, cudaStream_t st) {
-  constexpr size_t smem = eo_smem_bytes<P>();
+  constexpr size_t smem = eo_block_smem<P, CT>(EoCfg<P>::EPB);
   static bool attr_done = false;
   if (!attr_done) {
-    SDG_CUDA_TRY(cudaFuncSetAttribute(stage_eo_kernel<P>,
+    SDG_CUDA_TRY(cudaFuncSetAttribute(stage_eo_kernel<P, CT>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SDG_CUDA_TRY(cudaFuncSetAttribute(stage_eo_kernel<P, CT>,
+                                      cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      (int)cudaSharedmemCarveoutMaxShared));
     attr_done = true;
   }
   const long long nblk = (a.elem_count + EoCfg<P>::EPB - 1) / EoCfg<P>::EPB;
   if (nblk <= 0) return SDG_OK;
   if (nblk > 0x7fffffffLL) return fail(SDG_ERR_INVALID_ARG, "too many elements");
-  stage_eo_kernel<P><<<(unsigned)nblk, EoCfg<P>::THREADS, smem, st>>>(a);
+  stage_eo_kernel<P, CT><<<(unsigned)nblk, EoCfg<P>::THREADS, smem, st>>>(a);
   SDG_CUDA_TRY(cudaGetLastError());
   return SDG_OK;
 }

@@ -11,11 +11,15 @@ namespace sdg {
 template <int P>
 int launch_stage_order(int prec, int opt, const StageArgs& a, cudaStream_t st) {
   constexpr bool kCanSplit = (P > 7);
-  // EVENODD: its own FP64 body; the FP32 form runs the OPT1 order for it
+  // EVENODD: the even-odd bodies (FP64 and FP32); the emulated form runs its
+  // own line body for every opt type
   const bool split = kCanSplit && (opt != SDG_OPT_GENERAL);
   if (prec == SDG_PREC_FP64_EMU) return launch_stage_emu_impl<P>(a, st);
+  if (opt == SDG_OPT_EVENODD) {
+    if (prec == SDG_PREC_FP64) return launch_stage_eo_impl<P, double>(a, st);
+    return launch_stage_eo_impl<P, float>(a, st);
+  }
   if (prec == SDG_PREC_FP64) {
-    if (opt == SDG_OPT_EVENODD) return launch_stage_eo_impl<P>(a, st);
     if (split) return launch_stage_impl<P, double, double, kCanSplit>(a, st);
     return launch_stage_impl<P, double, double, false>(a, st);
   }

@@ -41,7 +41,7 @@ PREC_FP64_EMU = 2
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_size_t), ("max_active", C.c_int),
                 ("max_window_steps", C.c_int), ("threads", C.c_int),
-                ("epb_by_order", C.c_int * 16)]
+                ("epb_by_order", C.c_int * 16), ("opt", C.c_int)]
 
 
 class Request(C.Structure):
@@ -142,6 +142,7 @@ def _load() -> C.CDLL:
         "sdg_ensemble_init_blob": ([_vp, _i, _dp, _d, _dp], _i),
         "sdg_ensemble_tune": ([_vp], _i),
         "sdg_ensemble_set_epb": ([_vp, _i, _i], _i),
+        "sdg_ensemble_set_opt": ([_vp, _i], _i),
         "sdg_ensemble_set_threads": ([_vp, _i], _i),
         "sdg_ensemble_get_config": ([_vp, _ip, C.POINTER(_i), C.POINTER(_i)], _i),
         "sdg_ensemble_step": ([_vp, _i], _i),
@@ -519,6 +520,10 @@ class Ensemble:
     def set_threads(self, threads) -> None:
         _check(lib.sdg_ensemble_set_threads(self._h, threads), "sdg_ensemble_set_threads")
 
+    def set_opt(self, opt) -> None:
+        """OPT_GENERAL/OPT_OPT1 (default): node body; OPT_EVENODD: even-odd body."""
+        _check(lib.sdg_ensemble_set_opt(self._h, opt), "sdg_ensemble_set_opt")
+
     def config(self) -> dict:
         epb = np.zeros(12, dtype=np.int32)
         th, gr = _i(), _i()
@@ -570,10 +575,11 @@ class Server:
     """Continuous-batching solve server (sdg_server_* in include/sdg_advect.h)."""
 
     def __init__(self, ops_by_order, hbm_budget_bytes=64 << 30, max_active=512,
-                 max_window_steps=8, threads=0, device=0):
+                 max_window_steps=8, threads=0, device=0, opt=0):
         self._arrs, D, L, X = _order_table(ops_by_order)
         cfg = ServerConfig()
         cfg.device = device
+        cfg.opt = opt
         cfg.hbm_budget_bytes = int(hbm_budget_bytes)
         cfg.max_active = max_active
         cfg.max_window_steps = max_window_steps

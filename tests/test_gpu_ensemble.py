@@ -29,19 +29,46 @@ def build(members, seed0=100):
     return ens, fields, dts, ops
 
 
-def standalone(dims, p, fields, dt, ops, nstep):
-    s = sdg.Solver(*dims, p, ops[p][1], ops[p][3], opt=sdg.OPT_GENERAL, precision=sdg.PREC_FP32)
+def standalone(dims, p, fields, dt, ops, nstep, opt=sdg.OPT_GENERAL):
+    s = sdg.Solver(*dims, p, ops[p][1], ops[p][3], opt=opt, precision=sdg.PREC_FP32)
     s.upload(*fields)
     s.step(dt, nstep)
     return s.download()
 
 
-def test_members_equal_the_standalone_fp32_solver_bitwise():
+@pytest.mark.parametrize("opt", [sdg.OPT_EVENODD, sdg.OPT_GENERAL])
+def test_members_equal_the_standalone_fp32_solver_bitwise(opt):
+    """Node body (the default, GENERAL running sums) and even-odd body."""
     ens, fields, dts, ops = build(MEMBERS)
+    if opt == sdg.OPT_EVENODD:
+        ens.set_opt(opt)
     ens.step(4)
     for i, (dims, p) in enumerate(MEMBERS):
-        want = standalone(dims, p, fields[i], dts[i], ops, 4)
+        want = standalone(dims, p, fields[i], dts[i], ops, 4, opt)
         assert np.array_equal(ens.download(i), want), (i, dims, p)
+
+
+def test_switching_the_body_mid_run_keeps_the_state():
+    ens, fields, dts, ops = build(MEMBERS[:3], seed0=150)
+    ens.set_opt(sdg.OPT_EVENODD)
+    ens.step(2)
+    ens.set_opt(sdg.OPT_GENERAL)
+    ens.step(1)
+    ens.set_opt(sdg.OPT_EVENODD)
+    ens.step(1)
+    for i, (dims, p) in enumerate(MEMBERS[:3]):
+        s = sdg.Solver(*dims, p, ops[p][1], ops[p][3], opt=sdg.OPT_EVENODD,
+                       precision=sdg.PREC_FP32)
+        s.upload(*fields[i])
+        s.step(dts[i], 2)
+        q = s.download()
+        g = sdg.Solver(*dims, p, ops[p][1], ops[p][3], opt=sdg.OPT_GENERAL,
+                       precision=sdg.PREC_FP32)
+        g.upload(q, *fields[i][1:])
+        g.step(dts[i], 1)
+        s.upload(g.download(), *fields[i][1:])
+        s.step(dts[i], 1)
+        assert np.array_equal(ens.download(i), s.download()), i
 
 
 def test_members_within_fp32_tolerance_of_fp64_oracle():

@@ -105,6 +105,13 @@ def test_solver_run_matches_oracle(p, dims, nstep, ic, prec):
     assert rel_l2(q, c.oracle_run(nstep)) <= TOL_RUN
 
 
+@pytest.mark.parametrize("p", range(1, 16))
+def test_fp32_evenodd_tendency(p):
+    c = Case(*mesh_dims(p), p, ic="blob")
+    dq = solver_for(c, opt=sdg.OPT_EVENODD, prec=sdg.PREC_FP32).tendency()
+    assert rel_l2(dq, c.oracle_tend()) <= TOL_FP32
+
+
 @pytest.mark.parametrize("prec", [sdg.PREC_FP64, sdg.PREC_FP32, sdg.PREC_FP64_EMU])
 def test_pipelined_host_solves_equal_plain_solves(prec):
     dims, p, nstep = (3, 2, 4), 5, 3
@@ -392,9 +399,10 @@ def test_check_mesh_accepts_reference_mesh_and_rejects_others():
 
 
 @pytest.mark.parametrize("p", [2, 5, 7, 11])
-def test_fp32_compute_form_error_and_mass(p):
+@pytest.mark.parametrize("opt", [sdg.OPT_OPT1, sdg.OPT_EVENODD])
+def test_fp32_compute_form_error_and_mass(p, opt):
     c = Case(*mesh_dims(p), p, ic="blob")
-    s = solver_for(c, prec=sdg.PREC_FP32)
+    s = solver_for(c, opt=opt, prec=sdg.PREC_FP32)
     nstep = 10
     s.step(c.dt, nstep)
     q = s.download()

@@ -28,9 +28,26 @@ def req(dims, p, nstep, seed):
                 centre=prm["centre"], sigma=0.1, velocity=vel)
 
 
-def test_result_is_the_same_alone_and_in_the_mix(ops):
+def mixed_ops(ops):
+    """Order 3 with a D1D that lacks the centro-symmetry: that order runs the
+    node body while the others run the even-odd body (the mixed kernel)."""
+    out = dict(ops)
+    x, D, Dt, L = ops[3]
+    bad = D.copy()
+    bad[1] *= 1.0 + 1e-9
+    out[3] = (x, bad, Dt, L)
+    return out
+
+
+@pytest.mark.parametrize("body", ["evenodd", "node", "mixed"])
+def test_result_is_the_same_alone_and_in_the_mix(ops, body):
     target = req((3, 4, 2), 5, 40, 11)
-    srv = sdg.Server(ops)
+    if body == "node":
+        srv = sdg.Server(ops)
+    elif body == "mixed":
+        srv = sdg.Server(mixed_ops(ops), opt=sdg.OPT_EVENODD)
+    else:
+        srv = sdg.Server(ops, opt=sdg.OPT_EVENODD)
     alone, _ = None, None
     t = srv.submit(**target, want_state=True)
     res, alone = srv.wait(t)
@@ -53,9 +70,10 @@ def test_result_is_the_same_alone_and_in_the_mix(ops):
     srv.close()
 
 
-def test_served_result_matches_fp64_oracle_within_fp32_tolerance(ops):
+@pytest.mark.parametrize("opt", [0, sdg.OPT_EVENODD])
+def test_served_result_matches_fp64_oracle_within_fp32_tolerance(ops, opt):
     r = req((3, 2, 3), 3, 20, 31)
-    srv = sdg.Server(ops)
+    srv = sdg.Server(ops, opt=opt)
     _, q = srv.wait(srv.submit(**r, want_state=True))
     srv.close()
     p = r["p"]
