@@ -68,10 +68,19 @@ struct EoCfg {
 // Dynamic shared memory of one block with nloc elements: the three scaled
 // direction tables, then per element q, F_x (later the line-result sums), F_y,
 // F_z and the 6 Nfp face fluxes, then the neighbour indices.
+// The FP64 body does not stage q: the face flux and the RK update read it
+// from global memory (L1 / L2 hits after phase 0), which leaves room for a
+// third resident block.
+template <typename CT>
+__host__ __device__ constexpr bool eo_stages_q() {
+  return sizeof(CT) == 4;
+}
+
 template <int P, typename CT>
 __host__ __device__ constexpr size_t eo_block_smem(int nloc) {
   using O = Ord<P>;
-  return sizeof(CT) * (size_t)(3 * EoShape<P>::TE + nloc * (4 * O::NP + O::NFT)) +
+  return sizeof(CT) * (size_t)(3 * EoShape<P>::TE +
+                               nloc * ((eo_stages_q<CT>() ? 4 : 3) * O::NP + O::NFT)) +
          sizeof(int) * 6 * (size_t)nloc;
 }
 
@@ -98,9 +107,10 @@ __device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, C
   CT fm = CT(0);
   if constexpr (Sh::ODD != 0) fm = F[H * S];
   const CT gs = gm + gp, gd = gm - gp;
-  // rows unrolled up to p = 7; above that a rolled loop keeps the 2H line
-  // values and the row sums within the register budget
-  constexpr int kRowUnroll = (N <= 8) ? H : 1;
+  // rows unrolled up to p = 7 in FP32 and p = 4 in FP64; above that a rolled
+  // loop keeps the 2H line values and the row sums within the register budget
+  // (85 registers for three resident FP64 blocks)
+  constexpr int kRowUnroll = (N <= (sizeof(CT) == 8 ? 5 : 8)) ? H : 1;
 #pragma unroll kRowUnroll
   for (int i = 0; i < H; i++) {
     CT e = T[Sh::OFF_E + i * H] * s[0];
@@ -140,8 +150,9 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   constexpr bool kF64 = sizeof(CT) == 8;
   const int T = blockDim.x;
   CT* sT = reinterpret_cast<CT*>(smem);  // 3 directions x TE
-  CT* sq = sT + 3 * TE;
-  CT* sFx = sq + nloc * NP;  // F_x, then the running sum of the line results
+  constexpr bool kSQ = eo_stages_q<CT>();
+  CT* sq = sT + 3 * TE;      // q (FP32 body only)
+  CT* sFx = sq + (kSQ ? nloc * NP : 0);  // F_x, then the running sum of the line results
   CT* sFy = sFx + nloc * NP;
   CT* sFz = sFy + nloc * NP;
   CT* sf = sFz + nloc * NP;
@@ -178,7 +189,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
     snb[t] = (int)neighbor(a.box, eb + t / 6, t % 6);
   for (int t = threadIdx.x; t < nloc * NP; t += T) {
     const CT qq = to_ct<CT>(qin[g0 + t]);
-    sq[t] = qq;
+    if constexpr (kSQ) sq[t] = qq;
     sFx[t] = qq * gu[g0 + t];
     sFy[t] = qq * gv[g0 + t];
     sFz[t] = qq * gw[g0 + t];
@@ -197,7 +208,11 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
     const long long gP = (long long)snb[6 * le + f] * NP + nP;
     const CT* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
     const CT uM = gvel[gM], uP = gvel[gP];
-    const CT qM = sq[le * NP + nM];
+    CT qM;
+    if constexpr (kSQ)
+      qM = sq[le * NP + nM];
+    else
+      qM = to_ct<CT>(qin[gM]);
     const CT qP = to_ct<CT>(qin[gP]);
     const CT a2 = abs_ct(uP + uM);
     const CT tw = (sg > 0) ? CT(2) : CT(-2);
@@ -245,7 +260,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
       double inc, qv = 0.0;
       if constexpr (kF64) {
         inc = sFx[n] + v;
-        qv = sq[n];
+        qv = qin[g];
       } else {
         inc = f32_to_f64_bits(sFx[n] + v);
       }
@@ -263,9 +278,10 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
 
 // FP32: at least 4 resident blocks of 256 (registers capped at 64), since
 // the FP32 body issues few instructions per byte and needs the warps to hide
-// memory latency; FP64 is bound by the FP64 pipe and keeps its registers.
+// memory latency.  FP64: 3 blocks (85 registers), so that a block in its load
+// or flux phase leaves two others feeding the FP64 pipe.
 template <int P, typename CT>
-__global__ void __launch_bounds__(EoCfg<P>::THREADS, sizeof(CT) == 4 ? 4 : 1)
+__global__ void __launch_bounds__(EoCfg<P>::THREADS, sizeof(CT) == 4 ? 4 : 3)
     stage_eo_kernel(const StageArgs a) {
   constexpr int EPB = EoCfg<P>::EPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
