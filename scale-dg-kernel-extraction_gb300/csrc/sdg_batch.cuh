@@ -3,10 +3,12 @@
 //
 // Every box is an instance with its own order p, size, dt, rotating state
 // buffers and velocity.  A work item is one block's worth of consecutive
-// elements of one instance.  The persistent kernel's blocks pull items from a
-// global counter, resolve the instance's buffers for the stage, and run the
-// same fused stage body as the single-box solver (stage_block, FP32 compute,
-// FP64 state), dispatched on the instance's order.  Each instance's current
+// elements of one instance.  The persistent kernel's blocks take items
+// round-robin from the list (sorted by order), prefetch the next item's
+// instance header into shared memory while computing the current one, resolve
+// the instance's buffers for the stage, and run the same fused stage body as
+// the single-box solver (stage_block or stage_eo_block, FP32 compute, FP64
+// state), dispatched on the instance's order.  Each instance's current
 // buffer index lives on the device and is advanced by a tiny kernel after
 // stage 3, so one captured CUDA graph replays every step.
 #pragma once
@@ -56,12 +58,11 @@ inline void batch_stage_factors(BatchInst& I) {
   }
 }
 
-// Launches one stage over `n_items` items; counter must be zero on entry.
+// Launches one stage over `n_items` items.
 // mode: 0 all instances run the node body, 1 all the even-odd body, 2 mixed
 // (batch_mode below).
 int batch_stage_launch(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,
-                       int* d_counter, int grid, int threads, size_t smem, int mode,
-                       cudaStream_t st);
+                       int grid, int threads, size_t smem, int mode, cudaStream_t st);
 template <typename It, typename Get>
 inline int batch_mode(It begin, It end, Get eo_of) {
   bool any_eo = false, any_node = false;

@@ -21,19 +21,51 @@ __device__ __forceinline__ void run_order(const StageArgs& a, const BatchItem& w
     stage_block<P, float, float, false>(a, w.e_begin, w.e_count, smem);
 }
 
+// 32-bit words of an instance header, copied into shared memory by as many
+// threads.
+constexpr int kInstWords = (int)(sizeof(BatchInst) / 4);
+static_assert(sizeof(BatchInst) % 4 == 0, "instance header is copied as 32-bit words");
+static_assert(kInstWords < 128, "the smallest block must copy the header in one pass");
+
+// Items are assigned round-robin (block b runs items b, b + G, b + 2G, ...;
+// the list is sorted by order, so every block gets a similar mix).  The next
+// item's instance header is fetched into shared memory while the current item
+// computes, and the item after that into a register, so that a block never
+// waits on the item -> instance -> data chain of dependent loads.
 template <int MODE>
 __global__ void __launch_bounds__(kBatchThreadsMax)
     batch_stage_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
-                       int n_items, int stage, int* counter) {
+                       int n_items, int stage) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int s_item;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
-    __syncthreads();
-    const int it = s_item;
-    if (it >= n_items) return;  // uniform across the block
-    const BatchItem w = items[it];
-    const BatchInst& I = insts[w.inst];
+  __shared__ __align__(16) BatchInst s_inst[2];
+  __shared__ BatchItem s_items[2];
+  const int G = gridDim.x, tid = threadIdx.x;
+  int it = blockIdx.x;
+  if (it >= n_items) return;  // uniform across the block
+  // prologue: the first item, its header, and the second item
+  if (tid == 0) {
+    s_items[0] = items[it];
+    if (it + G < n_items) s_items[1] = items[it + G];
+  }
+  __syncthreads();
+  if (tid < kInstWords)
+    reinterpret_cast<uint32_t*>(&s_inst[0])[tid] =
+        reinterpret_cast<const uint32_t*>(insts + s_items[0].inst)[tid];
+  __syncthreads();
+
+  for (int k = 0; it < n_items; k++, it += G) {
+    const int slot = k & 1;
+    const bool has_next = it + G < n_items, has_next2 = it + 2 * G < n_items;
+    // prefetch, consumed after this item: the next item's header words and
+    // the item after it
+    uint32_t hw = 0;
+    BatchItem nn{};
+    if (has_next && tid < kInstWords)
+      hw = reinterpret_cast<const uint32_t*>(insts + s_items[slot ^ 1].inst)[tid];
+    if (has_next2 && tid == blockDim.x - 1) nn = items[it + 2 * G];
+
+    const BatchItem w = s_items[slot];
+    const BatchInst& I = s_inst[slot];
     if (I.active) {
       const int s0 = I.cur, s1 = (s0 + 1) % 3, s2 = (s0 + 2) % 3;
       StageArgs a;
@@ -79,7 +111,11 @@ __global__ void __launch_bounds__(kBatchThreadsMax)
         default: break;
       }
     }
-    __syncthreads();  // the next item reuses shared memory and s_item
+    // every read of this item's slots happened before the body's barriers
+    __syncthreads();
+    if (has_next && tid < kInstWords) reinterpret_cast<uint32_t*>(&s_inst[slot ^ 1])[tid] = hw;
+    if (has_next2 && tid == blockDim.x - 1) s_items[slot] = nn;
+    __syncthreads();  // the next item's header and the dynamic shared memory are ready
   }
 }
 
@@ -172,15 +208,14 @@ int batch_blocks_per_sm(int threads, size_t smem, int mode) {
 }
 
 int batch_stage_launch(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,
-                       int* d_counter, int grid, int threads, size_t smem, int mode,
-                       cudaStream_t st) {
+                       int grid, int threads, size_t smem, int mode, cudaStream_t st) {
   if (n_items <= 0) return SDG_OK;
   if (mode == 1)
-    batch_stage_kernel<1><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage, d_counter);
+    batch_stage_kernel<1><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage);
   else if (mode == 2)
-    batch_stage_kernel<2><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage, d_counter);
+    batch_stage_kernel<2><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage);
   else
-    batch_stage_kernel<0><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage, d_counter);
+    batch_stage_kernel<0><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage);
   SDG_CUDA_TRY(cudaGetLastError());
   return SDG_OK;
 }

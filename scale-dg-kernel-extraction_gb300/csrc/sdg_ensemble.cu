@@ -1,6 +1,6 @@
 // Ensemble of independent boxes advanced together (sdg_ensemble_* in
 // include/sdg_advect.h): all instances live in one device arena; a step is a
-// CUDA graph of [reset counters, 3 persistent stage launches, advance].
+// CUDA graph of [3 persistent stage launches, advance].
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -20,7 +20,6 @@ struct sdg_ensemble {
   BatchInst* d_inst = nullptr;
   BatchItem* d_items = nullptr;
   int n_items = 0;
-  int* d_counter = nullptr;        // 3 stage counters
   void* arena = nullptr;
   float* d_ops[kBatchMaxOrder + 1][3] = {};  // D1D, Lift, even-odd tables (FP32)
   bool use_eo = false;             // even-odd body (where the operators allow it)
@@ -48,7 +47,6 @@ void free_ensemble(sdg_ensemble* e) {
   if (e->graph) cudaGraphExecDestroy(e->graph);
   cudaFree(e->d_inst);
   cudaFree(e->d_items);
-  cudaFree(e->d_counter);
   cudaFree(e->arena);
   for (int p = 0; p <= kBatchMaxOrder; p++) {
     cudaFree(e->d_ops[p][0]);
@@ -98,10 +96,9 @@ int build_items(sdg_ensemble* e, const std::vector<int>* subset = nullptr) {
 }
 
 int enqueue_step(sdg_ensemble* e) {
-  SDG_CUDA_TRY(cudaMemsetAsync(e->d_counter, 0, 3 * sizeof(int), e->stream));
   for (int s = 0; s < 3; s++)
-    SDG_TRY(batch_stage_launch(e->d_inst, e->d_items, e->n_items, s, e->d_counter + s, e->grid,
-                               e->threads, e->smem, e->mode, e->stream));
+    SDG_TRY(batch_stage_launch(e->d_inst, e->d_items, e->n_items, s, e->grid, e->threads,
+                               e->smem, e->mode, e->stream));
   return batch_advance_launch(e->d_inst, e->n, e->stream);
 }
 
@@ -140,10 +137,9 @@ int time_stage0(sdg_ensemble* e, float* ms) {
   float best = 1e30f;
   for (int r = 0; r < 3; r++) {
     // stage 0 reads q[cur] and writes q[cur+1]: repeating it leaves the state
-    SDG_CUDA_TRY(cudaMemsetAsync(e->d_counter, 0, sizeof(int), e->stream));
     SDG_CUDA_TRY(cudaEventRecord(a, e->stream));
-    SDG_TRY(batch_stage_launch(e->d_inst, e->d_items, e->n_items, 0, e->d_counter, e->grid,
-                               e->threads, e->smem, e->mode, e->stream));
+    SDG_TRY(batch_stage_launch(e->d_inst, e->d_items, e->n_items, 0, e->grid, e->threads,
+                               e->smem, e->mode, e->stream));
     SDG_CUDA_TRY(cudaEventRecord(b, e->stream));
     SDG_CUDA_TRY(cudaEventSynchronize(b));
     float t = 0.f;
@@ -253,7 +249,6 @@ int sdg_ensemble_create(sdg_ensemble** out, int n, const int* dims, const int* o
   ce = cudaMalloc(&e->d_inst, sizeof(BatchInst) * n);
   if (ce == cudaSuccess)
     ce = cudaMemcpy(e->d_inst, e->inst.data(), sizeof(BatchInst) * n, cudaMemcpyHostToDevice);
-  if (ce == cudaSuccess) ce = cudaMalloc(&e->d_counter, 3 * sizeof(int));
   if (ce != cudaSuccess) return bail(cuda_fail(ce, "ensemble tables", __FILE__, __LINE__));
   int st = build_items(e);
   if (st != SDG_OK) return bail(st);

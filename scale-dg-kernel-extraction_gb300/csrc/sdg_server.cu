@@ -68,7 +68,6 @@ struct sdg_server {
   BatchItem* d_items = nullptr;
   int d_items_cap = 0;
   int n_items = 0;
-  int* d_counter = nullptr;
   size_t smem = 0;
   int grid = 0;
   int mode = 0;  // batch kernel body mode of the active set (batch_mode)
@@ -184,10 +183,9 @@ int rebuild_tables(sdg_server* s) {
 int run_steps(sdg_server* s, int nsteps) {
   const int n = (int)s->active.size();
   for (int k = 0; k < nsteps; k++) {
-    SDG_CUDA_TRY(cudaMemsetAsync(s->d_counter, 0, 3 * sizeof(int), s->stream));
     for (int st = 0; st < 3; st++)
-      SDG_TRY(batch_stage_launch(s->d_inst, s->d_items, s->n_items, st, s->d_counter + st,
-                                 s->grid, s->threads, s->smem, s->mode, s->stream));
+      SDG_TRY(batch_stage_launch(s->d_inst, s->d_items, s->n_items, st, s->grid, s->threads,
+                                 s->smem, s->mode, s->stream));
     SDG_TRY(batch_advance_launch(s->d_inst, n, s->stream));
     s->launches += 4;
   }
@@ -346,7 +344,6 @@ int sdg_server_create(sdg_server** out, const sdg_server_config* cfg,
       cudaFree(s->d_ops[p][2]);
       cudaFree(s->d_x1D[p]);
     }
-    cudaFree(s->d_counter);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return st;
@@ -359,7 +356,6 @@ int sdg_server_create(sdg_server** out, const sdg_server_config* cfg,
     uint64_t thresh = UINT64_MAX;
     ce = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &thresh);
   }
-  if (ce == cudaSuccess) ce = cudaMalloc(&s->d_counter, 3 * sizeof(int));
   if (ce == cudaSuccess) {
     // admission by free HBM: never promise more than 90% of what is free now
     size_t free_b = 0, total_b = 0;
@@ -521,7 +517,6 @@ int sdg_server_destroy(sdg_server* s) {
   }
   cudaFree(s->d_inst);
   cudaFree(s->d_items);
-  cudaFree(s->d_counter);
   cudaStreamDestroy(s->stream);
   delete s;
   return SDG_OK;
