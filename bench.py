@@ -478,27 +478,50 @@ def bench_serving(sdg, args, rate=None):
     }
 
 
+class Replicas:
+    """Replica plumbing under torchrun: a gloo process group used only for the
+    barrier around the timed region and the max of the per-rank times.  The
+    path exchanges no data between GPUs: each rank advances its own box."""
+
+    def __init__(self, ws: int):
+        self.ws = ws
+        self.dist = None
+        if ws > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self) -> None:
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def tmax(self, t: float) -> float:
+        if self.dist is None:
+            return t
+        import torch
+        tt = torch.tensor([t], dtype=torch.float64)
+        self.dist.all_reduce(tt, op=self.dist.ReduceOp.MAX)
+        return float(tt.item())
+
+    def close(self) -> None:
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+def whole_job_rate(ws: int, ndof: int, steps: int, t_max: float) -> float:
+    """GDOF-updates/s of all replicas: every rank advanced ndof DOFs through
+    3*steps stages, and the job took the slowest rank's time."""
+    return ws * ndof * 3 * steps / t_max / 1e9
+
+
 def run_ours(args, ws, rank, local):
     import sdg
     if sdg.device_count() < 1:
         raise SystemExit("bench.py: no CUDA device")
     sdg.set_device(local)
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist  # plumbing for the barrier and the max only
-        dist.init_process_group("gloo")
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def tmax(t):
-        if dist is None:
-            return t
-        import torch
-        tt = torch.tensor([t], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        return float(tt.item())
+    rep = Replicas(ws)
+    barrier, tmax = rep.barrier, rep.tmax
 
     p, ne = args.p, args.ne
     wl = make_workload(p, ne, args.seed + rank)
@@ -508,7 +531,7 @@ def run_ours(args, ws, rank, local):
     s, t, clk = time_solver(sdg, wl, p, ne, PRECISIONS[args.precision], args.steps,
                             args.warmup, local, barrier, True, OPTS[args.opt])
     t = tmax(t)
-    value = ws * ndof * 3 * args.steps / t / 1e9
+    value = whole_job_rate(ws, ndof, args.steps, t)
     peaks = None if args.no_microbench else sdg.microbench_peaks()
     roof = roofline(args.precision, p, ne, ndof, t, args.steps, peaks, args.opt)
 
@@ -561,8 +584,7 @@ def run_ours(args, ws, rank, local):
         se.close()
 
     if rank != 0:
-        if dist is not None:
-            dist.destroy_process_group()
+        rep.close()
         return 0
 
     cpu = None
@@ -609,8 +631,7 @@ def run_ours(args, ws, rank, local):
     if ws == 1 and not args.no_sweep:
         line["order_sweep"] = bench_order_sweep(sdg, args)
     print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    rep.close()
     return 0
 
 
