@@ -373,7 +373,7 @@ def bench_ensemble(sdg, args):
 def bench_order_sweep(sdg, args):
     """Orders 1..15 at about 16.8M DOF (Ne per axis = round(256/(p+1))), the
     seeded blob workload, nstep steps: throughput of the FP64 (OPT1 order and
-    even-odd body), emulated-FP64 and FP32 forms, and the relative L2 error and mass drift of the latter two
+    even-odd body), emulated-FP64 and FP32 (node and even-odd body) forms, and the relative L2 error and mass drift of the latter two
     against the FP64 form (which matches the CPU oracle to 1e-12 per
     tendency, tested)."""
     import workloads as W
@@ -390,7 +390,8 @@ def bench_order_sweep(sdg, args):
         for name, prec, opt in (("fp64", sdg.PREC_FP64, sdg.OPT_OPT1),
                                 ("fp64eo", sdg.PREC_FP64, sdg.OPT_EVENODD),
                                 ("fp64emu", sdg.PREC_FP64_EMU, sdg.OPT_OPT1),
-                                ("fp32", sdg.PREC_FP32, sdg.OPT_OPT1)):
+                                ("fp32", sdg.PREC_FP32, sdg.OPT_OPT1),
+                                ("fp32eo", sdg.PREC_FP32, sdg.OPT_EVENODD)):
             s = sdg.Solver(ne, ne, ne, p, D, L, opt=opt, precision=prec)
             s.upload(q, u, v, w)
             ms = s.step_timed(dt, args.sweep_steps)
@@ -399,7 +400,7 @@ def bench_order_sweep(sdg, args):
             row[f"{name}_gdof_updates_per_s"] = ndof * 3 * args.sweep_steps / (ms / 1e3) / 1e9
             row[f"{name}_mass_drift"] = abs(W.mass(res[name], x, ne, ne, ne) - m0) / abs(m0)
         ref = res["fp64"]
-        for name in ("fp64eo", "fp64emu", "fp32"):
+        for name in ("fp64eo", "fp64emu", "fp32", "fp32eo"):
             row[f"{name}_rel_l2_vs_fp64"] = float(np.linalg.norm(res[name] - ref) /
                                                   np.linalg.norm(ref))
         out.append(row)

@@ -32,8 +32,11 @@ static_assert(kInstWords < 128, "the smallest block must copy the header in one 
 // item's instance header is fetched into shared memory while the current item
 // computes, and the item after that into a register, so that a block never
 // waits on the item -> instance -> data chain of dependent loads.
+// Register caps: the node body fits in 42 (three blocks of 512 threads an
+// SM); the even-odd modes are capped at 64 (two blocks), since the switch over
+// eleven orders otherwise makes the compiler keep the union of their needs.
 template <int MODE>
-__global__ void __launch_bounds__(kBatchThreadsMax)
+__global__ void __launch_bounds__(kBatchThreadsMax, MODE == 0 ? 3 : 2)
     batch_stage_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
                        int n_items, int stage) {
   extern __shared__ __align__(16) unsigned char smem[];

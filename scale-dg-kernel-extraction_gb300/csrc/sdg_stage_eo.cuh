@@ -59,9 +59,18 @@ struct EoShape {
   static constexpr int TE = OFF_B + H;                 // entries per direction
 };
 
-template <int P>
+// Threads per line in the line phases: the FP32 body splits a line's output
+// pairs between two threads (each forms the line's pair sums itself), which
+// halves the registers a thread needs and doubles the warps that hide memory
+// latency; the FP64 body is bound by the FP64 pipe and keeps one.
+template <typename CT>
+__host__ __device__ constexpr int eo_parts() {
+  return sizeof(CT) == 4 ? 2 : 1;
+}
+
+template <int P, typename CT = double>
 struct EoCfg {
-  static constexpr int THREADS = 256;
+  static constexpr int THREADS = 256 * eo_parts<CT>();
   static constexpr int EPB = (256 / Ord<P>::NQ2) > 0 ? 256 / Ord<P>::NQ2 : 1;
 };
 
@@ -76,11 +85,13 @@ __host__ __device__ constexpr bool eo_stages_q() {
   return sizeof(CT) == 4;
 }
 
+// (The FP32 body keeps the line-result sums in their own array, since two
+// threads share a line and one may write before the other has read.)
 template <int P, typename CT>
 __host__ __device__ constexpr size_t eo_block_smem(int nloc) {
   using O = Ord<P>;
-  return sizeof(CT) * (size_t)(3 * EoShape<P>::TE +
-                               nloc * ((eo_stages_q<CT>() ? 4 : 3) * O::NP + O::NFT)) +
+  constexpr int arrays = (eo_stages_q<CT>() ? 4 : 3) + (eo_parts<CT>() > 1 ? 1 : 0);
+  return sizeof(CT) * (size_t)(3 * EoShape<P>::TE + nloc * (arrays * O::NP + O::NFT)) +
          sizeof(int) * 6 * (size_t)nloc;
 }
 
@@ -92,11 +103,15 @@ __device__ __forceinline__ float abs_ct(float x) { return fabsf(x); }
 // One line: F (stride S) holds the line's N volume fluxes, T the direction's
 // scaled tables, gm / gp the face fluxes of the line's - and + faces.  The
 // N results go to emit(m, value) after all reads of F.
-template <int P, int S, typename CT, typename Emit>
+// With PARTS threads on a line, thread `part` produces the pairs of rows
+// [part * RPP, (part + 1) * RPP) (RPP = ceil(H / PARTS)) and the last part the
+// middle row of an odd N.
+template <int P, int S, int PARTS, typename CT, typename Emit>
 __device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, CT gm, CT gp,
-                                        Emit&& emit) {
+                                        int part, Emit&& emit) {
   using Sh = EoShape<P>;
   constexpr int N = Sh::N, H = Sh::H;
+  constexpr int RPP = (H + PARTS - 1) / PARTS;
   CT s[H], d[H];
 #pragma unroll
   for (int l = 0; l < H; l++) {
@@ -110,9 +125,11 @@ __device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, C
   // rows unrolled up to p = 7 in FP32 and p = 4 in FP64; above that a rolled
   // loop keeps the 2H line values and the row sums within the register budget
   // (85 registers for three resident FP64 blocks)
-  constexpr int kRowUnroll = (N <= (sizeof(CT) == 8 ? 5 : 8)) ? H : 1;
+  constexpr int kRowUnroll = (N <= (sizeof(CT) == 8 ? 5 : 8)) ? RPP : 1;
 #pragma unroll kRowUnroll
-  for (int i = 0; i < H; i++) {
+  for (int ii = 0; ii < RPP; ii++) {
+    const int i = part * RPP + ii;
+    if (PARTS > 1 && i >= H) break;
     CT e = T[Sh::OFF_E + i * H] * s[0];
 #pragma unroll
     for (int l = 1; l < H; l++) e = fma(T[Sh::OFF_E + i * H + l], s[l], e);
@@ -125,7 +142,7 @@ __device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, C
     emit(i, e + o);
     emit(N - 1 - i, o - e);
   }
-  if constexpr (Sh::ODD != 0) {
+  if (Sh::ODD != 0 && part == PARTS - 1) {
     CT o = T[Sh::OFF_O + H * H] * d[0];
 #pragma unroll
     for (int l = 1; l < H; l++) o = fma(T[Sh::OFF_O + H * H + l], d[l], o);
@@ -155,7 +172,9 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   CT* sFx = sq + (kSQ ? nloc * NP : 0);  // F_x, then the running sum of the line results
   CT* sFy = sFx + nloc * NP;
   CT* sFz = sFy + nloc * NP;
-  CT* sf = sFz + nloc * NP;
+  constexpr int PARTS = eo_parts<CT>();
+  CT* sAcc = (PARTS > 1) ? sFz + nloc * NP : sFx;  // line-result sums
+  CT* sf = sFz + nloc * NP * (PARTS > 1 ? 2 : 1);
   int* snb = reinterpret_cast<int*>(sf + nloc * NFT);
 
   const double* __restrict__ qin = a.q_in;
@@ -222,23 +241,28 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   }
   __syncthreads();
 
-  // phase 2x: lines along i, faces -x (3) and +x (1); results over F_x
-  for (int t = threadIdx.x; t < nloc * NQ2; t += T) {
-    const int le = t / NQ2, r = t - le * NQ2;
-    CT* F = sFx + le * NP + r * NQ;
+  // phase 2x: lines along i, faces -x (3) and +x (1); results into the sums
+  // (over F_x itself when one thread owns the line)
+  for (int t = threadIdx.x; t < nloc * NQ2 * PARTS; t += T) {
+    const int part = t % PARTS, lt = t / PARTS;
+    const int le = lt / NQ2, r = lt - le * NQ2;
+    const CT* F = sFx + le * NP + r * NQ;
+    CT* acc = sAcc + le * NP + r * NQ;
     const CT* fl = sf + le * NFT + r;
-    eo_line<P, 1>(F, sT, fl[3 * NFP], fl[1 * NFP], [&](int m, CT v) { F[m] = v; });
+    eo_line<P, 1, PARTS>(F, sT, fl[3 * NFP], fl[1 * NFP], part,
+                         [&](int m, CT v) { acc[m] = v; });
   }
   __syncthreads();
 
   // phase 2y: lines along j, faces -y (0) and +y (2); added into the sums
-  for (int t = threadIdx.x; t < nloc * NQ2; t += T) {
-    const int le = t / NQ2, r = t - le * NQ2;
+  for (int t = threadIdx.x; t < nloc * NQ2 * PARTS; t += T) {
+    const int part = t % PARTS, lt = t / PARTS;
+    const int le = lt / NQ2, r = lt - le * NQ2;
     const int off = le * NP + (r % NQ) + (r / NQ) * NQ2;
-    CT* acc = sFx + off;
+    CT* acc = sAcc + off;
     const CT* fl = sf + le * NFT + r;
-    eo_line<P, NQ>(sFy + off, sT + TE, fl[0], fl[2 * NFP],
-                   [&](int m, CT v) { acc[m * NQ] += v; });
+    eo_line<P, NQ, PARTS>(sFy + off, sT + TE, fl[0], fl[2 * NFP], part,
+                          [&](int m, CT v) { acc[m * NQ] += v; });
   }
   __syncthreads();
 
@@ -250,19 +274,21 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   const double* __restrict__ q0 = a.q0;
   const double rk_a = a.a, rk_b = a.b;
   const int tend_only = a.tend_only, b_is_one = a.b_is_one, a_nonzero = a.a_nonzero;
-  for (int t = threadIdx.x; t < nloc * NQ2; t += T) {
-    const int le = t / NQ2, r = t - le * NQ2;
+  for (int t = threadIdx.x; t < nloc * NQ2 * PARTS; t += T) {
+    const int part = t % PARTS, lt = t / PARTS;
+    const int le = lt / NQ2, r = lt - le * NQ2;
     const int off = le * NP + r;
     const CT* fl = sf + le * NFT + r;
-    eo_line<P, NQ2>(sFz + off, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], [&](int m, CT v) {
+    eo_line<P, NQ2, PARTS>(sFz + off, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], part,
+                           [&](int m, CT v) {
       const int n = off + m * NQ2;
       const long long g = g0 + n;
       double inc, qv = 0.0;
       if constexpr (kF64) {
-        inc = sFx[n] + v;
+        inc = sAcc[n] + v;
         qv = qin[g];
       } else {
-        inc = f32_to_f64_bits(sFx[n] + v);
+        inc = f32_to_f64_bits(sAcc[n] + v);
       }
       if (tend_only) {
         qout[g] = inc;
@@ -281,9 +307,9 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
 // memory latency.  FP64: 3 blocks (85 registers), so that a block in its load
 // or flux phase leaves two others feeding the FP64 pipe.
 template <int P, typename CT>
-__global__ void __launch_bounds__(EoCfg<P>::THREADS, sizeof(CT) == 4 ? 4 : 3)
+__global__ void __launch_bounds__(EoCfg<P, CT>::THREADS, sizeof(CT) == 4 ? 2 : 3)
     stage_eo_kernel(const StageArgs a) {
-  constexpr int EPB = EoCfg<P>::EPB;
+  constexpr int EPB = EoCfg<P, CT>::EPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const long long eb = a.elem_begin + (long long)blockIdx.x * EPB;
   const long long eend = a.elem_begin + a.elem_count;
@@ -294,7 +320,7 @@ __global__ void __launch_bounds__(EoCfg<P>::THREADS, sizeof(CT) == 4 ? 4 : 3)
 
 template <int P, typename CT>
 int launch_stage_eo_impl(const StageArgs& a, cudaStream_t st) {
-  constexpr size_t smem = eo_block_smem<P, CT>(EoCfg<P>::EPB);
+  constexpr size_t smem = eo_block_smem<P, CT>(EoCfg<P, CT>::EPB);
   static bool attr_done = false;
   if (!attr_done) {
     SDG_CUDA_TRY(cudaFuncSetAttribute(stage_eo_kernel<P, CT>,
@@ -304,10 +330,10 @@ int launch_stage_eo_impl(const StageArgs& a, cudaStream_t st) {
                                       (int)cudaSharedmemCarveoutMaxShared));
     attr_done = true;
   }
-  const long long nblk = (a.elem_count + EoCfg<P>::EPB - 1) / EoCfg<P>::EPB;
+  const long long nblk = (a.elem_count + EoCfg<P, CT>::EPB - 1) / EoCfg<P, CT>::EPB;
   if (nblk <= 0) return SDG_OK;
   if (nblk > 0x7fffffffLL) return fail(SDG_ERR_INVALID_ARG, "too many elements");
-  stage_eo_kernel<P, CT><<<(unsigned)nblk, EoCfg<P>::THREADS, smem, st>>>(a);
+  stage_eo_kernel<P, CT><<<(unsigned)nblk, EoCfg<P, CT>::THREADS, smem, st>>>(a);
   SDG_CUDA_TRY(cudaGetLastError());
   return SDG_OK;
 }
