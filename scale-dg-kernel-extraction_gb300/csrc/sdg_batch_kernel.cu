@@ -12,13 +12,13 @@ __constant__ double c_rk_b[3] = {1.0, 0.25, 2.0 / 3.0};
 // MODE 0: every instance runs the node body; 1: every instance the even-odd
 // body; 2: either, per instance.  Separate instantiations keep each body's
 // register budget (the combined one needs the larger of the two).
-template <int P, int MODE>
+template <int P, int MODE, int RK>
 __device__ __forceinline__ void run_order(const StageArgs& a, const BatchItem& w, int eo,
                                           unsigned char* smem) {
   if (MODE == 1 || (MODE == 2 && eo))
-    stage_eo_block<P, float>(a, w.e_begin, w.e_count, smem);
+    stage_eo_block<P, float, RK>(a, w.e_begin, w.e_count, smem);
   else
-    stage_block<P, float, float, false>(a, w.e_begin, w.e_count, smem);
+    stage_block<P, float, float, false, RK>(a, w.e_begin, w.e_count, smem);
 }
 
 // 32-bit words of an instance header, copied into shared memory by as many
@@ -35,7 +35,9 @@ static_assert(kInstWords < 128, "the smallest block must copy the header in one 
 // Register caps: the node body fits in 42 (three blocks of 512 threads an
 // SM); the even-odd modes are capped at 64 (two blocks), since the switch over
 // eleven orders otherwise makes the compiler keep the union of their needs.
-template <int MODE>
+// RK: the stage's update kind (kRkFirst for stage 1, kRkGeneral otherwise),
+// a template parameter so that each instantiation carries one variant.
+template <int MODE, int RK>
 __global__ void __launch_bounds__(kBatchThreadsMax, MODE == 0 ? 3 : 2)
     batch_stage_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
                        int n_items, int stage) {
@@ -100,17 +102,17 @@ __global__ void __launch_bounds__(kBatchThreadsMax, MODE == 0 ? 3 : 2)
         }
       }
       switch (I.p) {
-        case 1: run_order<1, MODE>(a, w, eo, smem); break;
-        case 2: run_order<2, MODE>(a, w, eo, smem); break;
-        case 3: run_order<3, MODE>(a, w, eo, smem); break;
-        case 4: run_order<4, MODE>(a, w, eo, smem); break;
-        case 5: run_order<5, MODE>(a, w, eo, smem); break;
-        case 6: run_order<6, MODE>(a, w, eo, smem); break;
-        case 7: run_order<7, MODE>(a, w, eo, smem); break;
-        case 8: run_order<8, MODE>(a, w, eo, smem); break;
-        case 9: run_order<9, MODE>(a, w, eo, smem); break;
-        case 10: run_order<10, MODE>(a, w, eo, smem); break;
-        case 11: run_order<11, MODE>(a, w, eo, smem); break;
+        case 1: run_order<1, MODE, RK>(a, w, eo, smem); break;
+        case 2: run_order<2, MODE, RK>(a, w, eo, smem); break;
+        case 3: run_order<3, MODE, RK>(a, w, eo, smem); break;
+        case 4: run_order<4, MODE, RK>(a, w, eo, smem); break;
+        case 5: run_order<5, MODE, RK>(a, w, eo, smem); break;
+        case 6: run_order<6, MODE, RK>(a, w, eo, smem); break;
+        case 7: run_order<7, MODE, RK>(a, w, eo, smem); break;
+        case 8: run_order<8, MODE, RK>(a, w, eo, smem); break;
+        case 9: run_order<9, MODE, RK>(a, w, eo, smem); break;
+        case 10: run_order<10, MODE, RK>(a, w, eo, smem); break;
+        case 11: run_order<11, MODE, RK>(a, w, eo, smem); break;
         default: break;
       }
     }
@@ -181,10 +183,30 @@ size_t batch_smem_bytes(int p, int epb, int eo) {
 }
 
 namespace {
+template <int MODE, int RK>
+int set_max_smem_one(size_t smem) {
+  SDG_CUDA_TRY(cudaFuncSetAttribute(batch_stage_kernel<MODE, RK>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  return SDG_OK;
+}
+
 template <int MODE>
 int set_max_smem_mode(size_t smem) {
-  SDG_CUDA_TRY(cudaFuncSetAttribute(batch_stage_kernel<MODE>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int st = set_max_smem_one<MODE, kRkFirst>(smem);
+  if (st != SDG_OK) return st;
+  return set_max_smem_one<MODE, kRkGeneral>(smem);
+}
+
+template <int MODE>
+int launch_mode(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,
+                int grid, int threads, size_t smem, cudaStream_t st) {
+  if (stage == 0)
+    batch_stage_kernel<MODE, kRkFirst><<<grid, threads, smem, st>>>(d_inst, d_items, n_items,
+                                                                    stage);
+  else
+    batch_stage_kernel<MODE, kRkGeneral><<<grid, threads, smem, st>>>(d_inst, d_items, n_items,
+                                                                      stage);
+  SDG_CUDA_TRY(cudaGetLastError());
   return SDG_OK;
 }
 }  // namespace
@@ -195,14 +217,20 @@ int batch_set_max_smem(size_t smem, int mode) {
   return set_max_smem_mode<0>(smem);
 }
 
+// Occupancy of the general-stage instantiation (the first-stage one has the
+// same shape and no more registers).
 int batch_blocks_per_sm(int threads, size_t smem, int mode) {
   int nb = 0;
   if (batch_set_max_smem(smem, mode) != SDG_OK) return 0;
-  cudaError_t ce = (mode == 1)
-      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<1>, threads, smem)
+  cudaError_t ce =
+      (mode == 1)
+          ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<1, kRkGeneral>,
+                                                          threads, smem)
       : (mode == 2)
-      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<2>, threads, smem)
-      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<0>, threads, smem);
+          ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<2, kRkGeneral>,
+                                                          threads, smem)
+          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<0, kRkGeneral>,
+                                                          threads, smem);
   if (ce != cudaSuccess) {
     cudaGetLastError();
     return 0;
@@ -213,14 +241,9 @@ int batch_blocks_per_sm(int threads, size_t smem, int mode) {
 int batch_stage_launch(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,
                        int grid, int threads, size_t smem, int mode, cudaStream_t st) {
   if (n_items <= 0) return SDG_OK;
-  if (mode == 1)
-    batch_stage_kernel<1><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage);
-  else if (mode == 2)
-    batch_stage_kernel<2><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage);
-  else
-    batch_stage_kernel<0><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, stage);
-  SDG_CUDA_TRY(cudaGetLastError());
-  return SDG_OK;
+  if (mode == 1) return launch_mode<1>(d_inst, d_items, n_items, stage, grid, threads, smem, st);
+  if (mode == 2) return launch_mode<2>(d_inst, d_items, n_items, stage, grid, threads, smem, st);
+  return launch_mode<0>(d_inst, d_items, n_items, stage, grid, threads, smem, st);
 }
 
 int batch_advance_launch(BatchInst* d_inst, int n_inst, cudaStream_t st) {

@@ -23,10 +23,49 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "sdg_df.cuh"
 #include "sdg_internal.h"
 
 namespace sdg {
+
+// RK update kinds of a stage, decided once per launch so that a node issues
+// only its own FP64 operations: a per-node select between an add and an FMA
+// would be if-converted into both, on the 1/64-rate FP64 pipe.
+//   kRkTend     q_out = the tendency increment (c = 1, no state update)
+//   kRkFirst    q_out = q + inc                 (b = 1, a = 0: stage 1)
+//   kRkGeneral  q_out = a q0 + (b q + inc)
+constexpr int kRkTend = 0, kRkFirst = 1, kRkGeneral = 2;
+
+__host__ __device__ inline int rk_kind(const StageArgs& a) {
+  return a.tend_only ? kRkTend : (a.b_is_one && !a.a_nonzero) ? kRkFirst : kRkGeneral;
+}
+
+template <int RK>
+__device__ __forceinline__ double rk_combine(double inc, double qv, double q0v, double ra,
+                                             double rb) {
+  if constexpr (RK == kRkFirst)
+    return qv + inc;
+  else
+    return fma(ra, q0v, fma(rb, qv, inc));
+}
+
+// Calls f(std::integral_constant<int, RK>{}) for the launch's RK kind.  A
+// caller that knows the kind at compile time passes it as FIXED (>= 0), and
+// only that variant is instantiated (the batched kernel, whose many order
+// bodies would otherwise triple).
+template <int FIXED = -1, typename F>
+__device__ __forceinline__ void with_rk_kind(int kind, F&& f) {
+  if constexpr (FIXED >= 0)
+    f(std::integral_constant<int, FIXED>{});
+  else if (kind == kRkTend)
+    f(std::integral_constant<int, kRkTend>{});
+  else if (kind == kRkFirst)
+    f(std::integral_constant<int, kRkFirst>{});
+  else
+    f(std::integral_constant<int, kRkGeneral>{});
+}
 
 template <int P>
 struct Ord {
@@ -152,7 +191,7 @@ __host__ __device__ constexpr size_t stage_block_smem(int nloc) {
 // stage.  The block size and nloc are runtime values, so the batched
 // persistent kernel can run any order and any elements-per-block choice
 // through the same body; `smem` holds stage_block_smem<P, CT>(nloc) bytes.
-template <int P, typename CT, typename VT, bool SPLIT3>
+template <int P, typename CT, typename VT, bool SPLIT3, int RKFIX = -1>
 __device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, int nloc,
                                             unsigned char* smem) {
   using O = Ord<P>;
@@ -237,44 +276,49 @@ __device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, in
     Ez = a.box.Es[2];
   }
   const CT* __restrict__ L = static_cast<const CT*>(a.Lift);
-  for (int t = threadIdx.x; t < nloc * NP; t += T) {
-    const int le = t / NP;
-    const int n = t - le * NP;
-    const int i = n % NQ;
-    const int j = (n / NQ) % NQ;
-    const int k = n / NQ2;
-    const CT* Fx = su + le * NP;
-    const CT* Fy = sv + le * NP;
-    const CT* Fz = sw + le * NP;
-    const CT dx = line_sum<NQ, SPLIT3, NQ>(sD + i, Fx + j * NQ + k * NQ2, 1);
-    const CT dy = line_sum<NQ, SPLIT3, NQ>(sD + j, Fy + i + k * NQ2, NQ);
-    const CT dz = line_sum<NQ, SPLIT3, NQ>(sD + k, Fz + i + j * NQ, NQ2);
-    const CT lf = lift_node<P>(L + n, sf + le * NFT, i, j, k);
-    const CT dq = -(((Ex * dx + Ey * dy) + Ez * dz) + lf);
-    const long long g = g0 + t;
-    if constexpr (sizeof(CT) == 8) {
-      if (a.tend_only) {
-        a.q_out[g] = (double)dq;
+  double* __restrict__ qout = a.q_out;
+  const double* __restrict__ q0 = a.q0;
+  const double ra = a.a, rb = a.b, rdt = a.dt;
+  const CT cdt = a.cdt_hi;
+  with_rk_kind<RKFIX>(rk_kind(a), [&](auto rkc) {
+    constexpr int RK = decltype(rkc)::value;
+    for (int t = threadIdx.x; t < nloc * NP; t += T) {
+      const int le = t / NP;
+      const int n = t - le * NP;
+      const int i = n % NQ;
+      const int j = (n / NQ) % NQ;
+      const int k = n / NQ2;
+      const CT* Fx = su + le * NP;
+      const CT* Fy = sv + le * NP;
+      const CT* Fz = sw + le * NP;
+      const CT dx = line_sum<NQ, SPLIT3, NQ>(sD + i, Fx + j * NQ + k * NQ2, 1);
+      const CT dy = line_sum<NQ, SPLIT3, NQ>(sD + j, Fy + i + k * NQ2, NQ);
+      const CT dz = line_sum<NQ, SPLIT3, NQ>(sD + k, Fz + i + j * NQ, NQ2);
+      const CT lf = lift_node<P>(L + n, sf + le * NFT, i, j, k);
+      const CT dq = -(((Ex * dx + Ey * dy) + Ez * dz) + lf);
+      const long long g = g0 + t;
+      if constexpr (sizeof(CT) == 8) {
+        // the reference's order, a*q0 + b*(q + dt*dqdt) (main.f90:69-73);
+        // stage 1 (a = 0, b = 1) is q + dt*dqdt exactly
+        if constexpr (RK == kRkTend) {
+          qout[g] = (double)dq;
+        } else if constexpr (RK == kRkFirst) {
+          qout[g] = qin[g] + rdt * (double)dq;
+        } else {
+          const double r = rb * (qin[g] + rdt * (double)dq);
+          qout[g] = ra * q0[g] + r;
+        }
       } else {
-        const double qv = qin[g];
-        double r = a.b * (qv + a.dt * (double)dq);
-        if (a.a_nonzero) r = a.a * a.q0[g] + r;
-        a.q_out[g] = r;
-      }
-    } else {
-      // FP32 form: the increment (b*dt)*dqdt is an FP32 product widened by
-      // bits; the state combination a*q0 + b*q + increment stays FP64
-      if (a.tend_only) {
-        a.q_out[g] = f32_to_f64_bits(dq);
-      } else {
-        const double inc = f32_to_f64_bits(a.cdt_hi * dq);
-        const double qv = qin[g];
-        double r = a.b_is_one ? qv + inc : fma(a.b, qv, inc);
-        if (a.a_nonzero) r = fma(a.a, a.q0[g], r);
-        a.q_out[g] = r;
+        // FP32 form: the increment (b*dt)*dqdt is an FP32 product widened by
+        // bits; the state combination a*q0 + b*q + increment stays FP64
+        if constexpr (RK == kRkTend)
+          qout[g] = f32_to_f64_bits(dq);
+        else
+          qout[g] = rk_combine<RK>(f32_to_f64_bits(cdt * dq), qin[g],
+                                   RK == kRkGeneral ? q0[g] : 0.0, ra, rb);
       }
     }
-  }
+  });
 }
 
 template <int P, typename CT, typename VT, bool SPLIT3>

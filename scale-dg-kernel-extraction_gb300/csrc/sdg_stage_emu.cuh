@@ -222,42 +222,46 @@ __global__ void __launch_bounds__(EmuCfg<P>::THREADS) stage_emu_kernel(const Sta
     const float2* __restrict__ Lt = static_cast<const float2*>(a.Lift);
     const float2* gl = sg + le * NFT;
     const dfl c_dt = df_make(a.cdt_hi, a.cdt_lo);
+    with_rk_kind(rk_kind(a), [&](auto rkc) {
+      constexpr int RK = decltype(rkc)::value;
 #pragma unroll 1
-    for (int k = 0; k < NQ; k++) {
-      const int s = i + PADL * (j + NQ * k);
-      const float2 acc = pl2[s];
-      dacc A;
-      A.s = acc.x;
-      A.c = acc.y;
+      for (int k = 0; k < NQ; k++) {
+        const int s = i + PADL * (j + NQ * k);
+        const float2 acc = pl2[s];
+        dacc A;
+        A.s = acc.x;
+        A.c = acc.y;
 #pragma unroll
-      for (int l = 0; l < NQ; l++) {
-        const float2 dd = sD[2 * NQ2 + l * NQ + k];
-        dacc_fma(A, df_make(dd.x, dd.y), df_make(Gl[l].x, Gl[l].y));
-      }
-      const float2 rr = sR[2 * NQ + k];
-      dacc_fma(A, df_make(rr.x, rr.y), base);
-      const int n = i + j * NQ + k * NQ2;
-      const int fidx[6] = {i + k * NQ, NFP + j + k * NQ, 2 * NFP + i + k * NQ,
-                           3 * NFP + j + k * NQ, 4 * NFP + i + j * NQ, 5 * NFP + i + j * NQ};
+        for (int l = 0; l < NQ; l++) {
+          const float2 dd = sD[2 * NQ2 + l * NQ + k];
+          dacc_fma(A, df_make(dd.x, dd.y), df_make(Gl[l].x, Gl[l].y));
+        }
+        const float2 rr = sR[2 * NQ + k];
+        dacc_fma(A, df_make(rr.x, rr.y), base);
+        const int n = i + j * NQ + k * NQ2;
+        const int fidx[6] = {i + k * NQ, NFP + j + k * NQ, 2 * NFP + i + k * NQ,
+                             3 * NFP + j + k * NQ, 4 * NFP + i + j * NQ, 5 * NFP + i + j * NQ};
 #pragma unroll
-      for (int f = 0; f < 6; f++) {
-        const float2 L = __ldg(Lt + n + f * NP);
-        const float2 gg = gl[fidx[f]];
-        dacc_fma(A, df_make(L.x, L.y), df_make(gg.x, gg.y));
+        for (int f = 0; f < 6; f++) {
+          const float2 L = __ldg(Lt + n + f * NP);
+          const float2 gg = gl[fidx[f]];
+          dacc_fma(A, df_make(L.x, L.y), df_make(gg.x, gg.y));
+        }
+        const dfl dq = df_neg(dacc_result(A));
+        const long long g = (eb + le) * NP + n;
+        if constexpr (RK == kRkTend) {
+          a.q_out[g] = f32_to_f64_bits(dq.hi) + f32_to_f64_bits(dq.lo);
+        } else {
+          const dfl inc = df_mul(c_dt, dq);  // (b*dt)*dqdt
+          const double ih = f32_to_f64_bits(inc.hi), il = f32_to_f64_bits(inc.lo);
+          const double qv = qin[g];
+          if constexpr (RK == kRkFirst)
+            a.q_out[g] = (qv + ih) + il;
+          else
+            a.q_out[g] = fma(a.a, a.q0[g], fma(a.b, qv, ih) + il);
+        }
       }
-      const dfl dq = df_neg(dacc_result(A));
-      const long long g = (eb + le) * NP + n;
-      if (a.tend_only) {
-        a.q_out[g] = f32_to_f64_bits(dq.hi) + f32_to_f64_bits(dq.lo);
-      } else {
-        const dfl inc = df_mul(c_dt, dq);  // (b*dt)*dqdt
-        const double ih = f32_to_f64_bits(inc.hi), il = f32_to_f64_bits(inc.lo);
-        const double qv = qin[g];
-        double rq = (a.b_is_one ? qv + ih : fma(a.b, qv, ih)) + il;
-        if (a.a_nonzero) rq = fma(a.a, a.q0[g], rq);
-        a.q_out[g] = rq;
-      }
-    }
+    });
   }
 }
 

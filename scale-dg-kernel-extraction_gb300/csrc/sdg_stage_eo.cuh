@@ -157,7 +157,7 @@ __device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, C
 // sums, scaled by eo_sDf / eo_sLf), with the increment widened by bits and
 // the RK combination in FP64.  Block size and nloc are runtime values, so the
 // batched persistent kernel can use the same body.
-template <int P, typename CT>
+template <int P, typename CT, int RKFIX = -1>
 __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb, int nloc,
                                                unsigned char* smem) {
   using O = Ord<P>;
@@ -273,41 +273,37 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   double* __restrict__ qout = a.q_out;
   const double* __restrict__ q0 = a.q0;
   const double rk_a = a.a, rk_b = a.b;
-  const int tend_only = a.tend_only, b_is_one = a.b_is_one, a_nonzero = a.a_nonzero;
-  for (int t = threadIdx.x; t < nloc * NQ2 * PARTS; t += T) {
-    const int part = t % PARTS, lt = t / PARTS;
-    const int le = lt / NQ2, r = lt - le * NQ2;
-    const int off = le * NP + r;
-    const CT* fl = sf + le * NFT + r;
-    eo_line<P, NQ2, PARTS>(sFz + off, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], part,
-                           [&](int m, CT v) {
-      const int n = off + m * NQ2;
-      const long long g = g0 + n;
-      double inc, qv = 0.0;
-      if constexpr (kF64) {
-        inc = sAcc[n] + v;
-        qv = qin[g];
-      } else {
-        inc = f32_to_f64_bits(sAcc[n] + v);
-      }
-      if (tend_only) {
-        qout[g] = inc;
-      } else {
-        if constexpr (!kF64) qv = qin[g];
-        double res = b_is_one ? qv + inc : fma(rk_b, qv, inc);
-        if (a_nonzero) res = fma(rk_a, q0[g], res);
-        qout[g] = res;
-      }
-    });
-  }
+  with_rk_kind<RKFIX>(rk_kind(a), [&](auto rkc) {
+    constexpr int RK = decltype(rkc)::value;
+    for (int t = threadIdx.x; t < nloc * NQ2 * PARTS; t += T) {
+      const int part = t % PARTS, lt = t / PARTS;
+      const int le = lt / NQ2, r = lt - le * NQ2;
+      const int off = le * NP + r;
+      const CT* fl = sf + le * NFT + r;
+      eo_line<P, NQ2, PARTS>(sFz + off, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], part,
+                             [&](int m, CT v) {
+        const int n = off + m * NQ2;
+        const long long g = g0 + n;
+        double inc;
+        if constexpr (kF64)
+          inc = sAcc[n] + v;
+        else
+          inc = f32_to_f64_bits(sAcc[n] + v);
+        if constexpr (RK == kRkTend)
+          qout[g] = inc;
+        else
+          qout[g] = rk_combine<RK>(inc, qin[g], RK == kRkGeneral ? q0[g] : 0.0, rk_a, rk_b);
+      });
+    }
+  });
 }
 
-// FP32: at least 4 resident blocks of 256 (registers capped at 64), since
-// the FP32 body issues few instructions per byte and needs the warps to hide
-// memory latency.  FP64: 3 blocks (85 registers), so that a block in its load
-// or flux phase leaves two others feeding the FP64 pipe.
+// Three resident blocks an SM.  FP32 (512 threads, registers capped at 42):
+// the body issues few instructions per byte and needs the warps to hide
+// memory latency.  FP64 (256 threads, 85 registers): a block in its load or
+// flux phase leaves two others feeding the FP64 pipe.
 template <int P, typename CT>
-__global__ void __launch_bounds__(EoCfg<P, CT>::THREADS, sizeof(CT) == 4 ? 2 : 3)
+__global__ void __launch_bounds__(EoCfg<P, CT>::THREADS, 3)
     stage_eo_kernel(const StageArgs a) {
   constexpr int EPB = EoCfg<P, CT>::EPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
