@@ -41,6 +41,24 @@ def test_fused_stage_tendency_matches_oracle(p, opt):
     assert rel_l2(dq, ref) <= TOL_TEND
 
 
+@pytest.mark.parametrize("p", [1, 4, 7, 12])
+@pytest.mark.parametrize("opt,prec,tol", [(sdg.OPT_OPT1, sdg.PREC_FP64, TOL_TEND),
+                                          (sdg.OPT_GENERAL, sdg.PREC_FP64, TOL_TEND),
+                                          (sdg.OPT_EVENODD, sdg.PREC_FP64, TOL_TEND),
+                                          (sdg.OPT_OPT1, sdg.PREC_FP64_EMU, TOL_TEND),
+                                          (sdg.OPT_OPT1, sdg.PREC_FP32, TOL_FP32),
+                                          (sdg.OPT_EVENODD, sdg.PREC_FP32, TOL_FP32)])
+def test_single_element_box_is_its_own_neighbour(p, opt, prec, tol):
+    """NeX = NeY = NeZ = 1: every face of the element meets its own opposite
+    face through the periodic wrap."""
+    c = Case(1, 1, 1, p, ic="blob")
+    s = solver_for(c, opt=opt, prec=prec)
+    ref = c.oracle_tend(sdg.OPT_GENERAL if opt == sdg.OPT_GENERAL else sdg.OPT_OPT1)
+    assert rel_l2(s.tendency(), ref) <= tol
+    s.step(c.dt, 3)
+    assert rel_l2(s.download(), c.oracle_run(3)) <= (TOL_RUN if tol == TOL_TEND else tol)
+
+
 @pytest.mark.parametrize("p", [1, 2, 5, 7, 8, 15])
 def test_evenodd_tendency_sine_and_anisotropic_box(p):
     """Even-odd stage: per-direction Escale / Fscale folding on a box with
@@ -213,6 +231,18 @@ def test_divlike_var5_matches_oracle(p):
         assert np.array_equal(dev[d].numpy(), got[d])
 
 
+@pytest.mark.parametrize("opt", ["OPT1", "GENERAL"])
+def test_dropin_single_element_box(opt):
+    c = Case(1, 1, 1, 9, ic="blob")
+    m = c.mesh
+    sdg.dg_optr_kernel_setup(opt)
+    dqdt = np.zeros(m.Np * m.NeA)
+    sdg.advect3d_eq_cal_tend(dqdt, c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, m.VMapM, m.VMapP,
+                             m.normal_fn, m.Escale, m.Fscale, m.Nq, m.Np, m.NfpTot, m.Ne, m.NeA)
+    ref = c.oracle_tend(O.OPT1 if opt == "OPT1" else O.GENERAL)
+    assert rel_l2(dqdt[: c.nown], ref) <= TOL_TEND
+
+
 def test_dropin_rejects_out_of_range_vmap():
     c = Case(2, 2, 2, 2, ic="blob")
     m = c.mesh
@@ -270,7 +300,8 @@ def test_dev_update_halo_and_rk_stage_match_oracle():
         assert np.max(np.abs(dqq.numpy() - ref)) <= 4e-16 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("dims,p", [((3, 2, 4), 3), ((1, 2, 3), 2), ((4, 4, 4), 7), ((2, 1, 1), 9)])
+@pytest.mark.parametrize("dims,p", [((3, 2, 4), 3), ((1, 2, 3), 2), ((4, 4, 4), 7), ((2, 1, 1), 9),
+                                    ((1, 1, 1), 5)])
 def test_device_mesh_equals_reference_mesh(dims, p):
     x, D, Dt, L = operators(p)
     m = O.Mesh(*dims, p, x)
