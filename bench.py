@@ -407,6 +407,68 @@ def bench_order_sweep(sdg, args):
     return out
 
 
+def bench_dropin(sdg, args, wl, fused_rate):
+    """The reference-shaped per-stage path on the bench workload, all on device
+    arrays: mesh arrays built on the device (sdg_mesh_setup_dev), then per step
+    q0 = q and three times update_halo(q), advect3d_eq_cal_tend(...) and the RK
+    stage, as main.f90:51-80 calls them.  Timed on the host around K steps
+    (queued asynchronously on one stream, launch cost included)."""
+    import ctypes as C
+    p, ne = args.p, args.ne
+    nq, np_ = p + 1, (p + 1) ** 3
+    ntf = 6 * nq * nq
+    ne3 = ne ** 3
+    nhalo = 6 * ne * ne
+    nea = ne3 + nhalo
+    nhn = nq * nq * nhalo
+    lib = sdg.lib
+    A = sdg.DeviceArray
+    vm, vp = A(n=ntf * ne3, dtype=np.int32), A(n=ntf * ne3, dtype=np.int32)
+    nf, fs = A(n=3 * ntf * ne3), A(n=ntf * ne3)
+    es, hm = A(n=3 * np_ * ne3), A(n=nhn, dtype=np.int32)
+    sdg._check(lib.sdg_mesh_setup_dev(ne, ne, ne, p, 1.0, 1.0, 1.0, None, vm.ptr, vp.ptr, nf.ptr,
+                                      es.ptr, fs.ptr, None, hm.ptr, None), "sdg_mesh_setup_dev")
+    fields = []
+    for key in ("q", "u", "v", "w"):
+        h = np.zeros(np_ * nea)
+        h[: np_ * ne3] = wl[key]
+        d = A(h)
+        sdg._check(lib.sdg_update_halo_dev(d.ptr, hm.ptr, np_, ne3, nhn, None), "update_halo")
+        fields.append(d)
+    q, u, v, w = fields
+    D, Dt, L = A(wl["D"]), A(wl["Dt"]), A(wl["L"])
+    dqdt, q0 = A(n=np_ * nea), A(n=np_ * ne3)
+    flux, err = A(n=ntf * ne3), A(np.zeros(1, dtype=np.int32))
+    dt = wl["dt"]
+
+    def step():
+        sdg._check(lib.sdg_memcpy_d2d_async(q0.ptr, q.ptr, 8 * np_ * ne3, None), "q0 = q")
+        for stage in range(3):
+            lib.sdg_update_halo_dev(q.ptr, hm.ptr, np_, ne3, nhn, None)
+            lib.sdg_advect3d_eq_cal_tend_dev(dqdt.ptr, q.ptr, u.ptr, v.ptr, w.ptr, D.ptr, Dt.ptr,
+                                             L.ptr, vm.ptr, vp.ptr, nf.ptr, es.ptr, fs.ptr, nq,
+                                             np_, ntf, ne3, nea, sdg.OPT_OPT1, flux.ptr, err.ptr,
+                                             None)
+            lib.sdg_rk_stage_dev(q.ptr, q0.ptr, dqdt.ptr, np_, ne3, stage, dt, None)
+
+    for _ in range(args.warmup):
+        step()
+    sdg.synchronize()
+    k = max(2, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        step()
+    sdg.synchronize()
+    t = time.perf_counter() - t0
+    assert err.numpy()[0] == 0
+    rate = np_ * ne3 * 3 * k / t / 1e9
+    return {"workload": f"same {ne}^3 p={p} box through the per-stage device entry points "
+                        "(update_halo, advect3d_eq_cal_tend_dev with VMapM/VMapP gathers, "
+                        "rk_stage_dev, OPT1 order) as the reference's loop calls them",
+            "gdof_updates_per_s": rate, "ms_per_step": 1e3 * t / k, "steps": k,
+            "launches_per_step": 13, "fused_over_dropin": fused_rate / rate}
+
+
 def bench_serving(sdg, args, rate=None):
     """Poisson arrivals of solves (Ne per axis U{4..32}, p U{2..11}, nstep
     U{10..500}, Gaussian tracer in a constant velocity, FP32 compute / FP64
@@ -622,6 +684,8 @@ def run_ours(args, ws, rank, local):
     }
     if other is not None:
         line["fp64_emulated"] = other
+    if ws == 1 and not args.no_dropin:
+        line["dropin"] = bench_dropin(sdg, args, wl, value)
     if ws == 1 and not args.no_ensemble:
         line["ensemble"] = bench_ensemble(sdg, args)
     if ws == 1 and not args.no_serving:
@@ -656,6 +720,8 @@ def main() -> int:
     ap.add_argument("--no-emu", action="store_true",
                     help="skip the emulated-FP64 measurement beside the FP64 headline")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-dropin", action="store_true",
+                    help="skip the per-stage drop-in path measurement")
     ap.add_argument("--batch-opt", choices=["general", "evenodd"], default="general",
                     help="stage body of the batched kernel (ensemble and serving)")
     ap.add_argument("--no-sweep", action="store_true")

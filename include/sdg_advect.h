@@ -451,6 +451,9 @@ int sdg_dev_alloc(size_t bytes, void** out);
 int sdg_dev_free(void* p);
 int sdg_memcpy_h2d(void* dst, const void* src, size_t bytes);
 int sdg_memcpy_d2h(void* dst, const void* src, size_t bytes);
+/* Device-to-device copy queued on `stream` (the q0 = q copy of the time loop,
+ * main.f90:54-57, for callers that drive the per-stage entry points). */
+int sdg_memcpy_d2d_async(void* dst, const void* src, size_t bytes, void* stream);
 int sdg_memset_dev(void* dst, int value, size_t bytes);
 
 /* Page-locked host memory for fast host<->device copies (cudaHostAlloc). */

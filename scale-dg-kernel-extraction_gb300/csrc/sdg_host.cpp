@@ -310,6 +310,13 @@ int sdg_memcpy_d2h(void* dst, const void* src, size_t bytes) {
   return SDG_OK;
 }
 
+int sdg_memcpy_d2d_async(void* dst, const void* src, size_t bytes, void* stream) {
+  if (!bytes) return SDG_OK;
+  if (!dst || !src) return fail(SDG_ERR_INVALID_ARG, "NULL pointer");
+  SDG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, as_stream(stream)));
+  return SDG_OK;
+}
+
 int sdg_memset_dev(void* dst, int value, size_t bytes) {
   if (!bytes) return SDG_OK;
   if (!dst) return fail(SDG_ERR_INVALID_ARG, "NULL pointer");

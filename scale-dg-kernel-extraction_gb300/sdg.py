@@ -132,6 +132,7 @@ def _load() -> C.CDLL:
         "sdg_dev_free": ([_vp], _i),
         "sdg_memcpy_h2d": ([_vp, _vp, C.c_size_t], _i),
         "sdg_memcpy_d2h": ([_vp, _vp, C.c_size_t], _i),
+        "sdg_memcpy_d2d_async": ([_vp, _vp, C.c_size_t, _vp], _i),
         "sdg_memset_dev": ([_vp, _i, C.c_size_t], _i),
         "sdg_pinned_alloc": ([C.c_size_t, C.POINTER(_vp)], _i),
         "sdg_pinned_free": ([_vp], _i),
