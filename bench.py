@@ -136,6 +136,10 @@ class OracleBox:
     fields with halos, the tendency of the initial state, and timed steps."""
 
     def __init__(self, wl, p, ne):
+        # the reference's OpenMP settings for a timed CPU run: one thread per
+        # core, bound close (read when the oracle library starts OpenMP)
+        os.environ.setdefault("OMP_PROC_BIND", "close")
+        os.environ.setdefault("OMP_PLACES", "cores")
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
         import workloads as W
@@ -462,11 +466,17 @@ def bench_dropin(sdg, args, wl, fused_rate):
     t = time.perf_counter() - t0
     assert err.numpy()[0] == 0
     rate = np_ * ne3 * 3 * k / t / 1e9
+    # the essential bytes plus the reference's geometry arrays, which this path
+    # streams: Escale 24 B per DOF, VMapM/VMapP/normal_fn/Fscale 40 B per face
+    # node (6/Nq face nodes per DOF)
+    bpd = BYTES_PER_DOF_UPDATE["fp64"] + 24.0 + 40.0 * 6.0 / nq
     return {"workload": f"same {ne}^3 p={p} box through the per-stage device entry points "
                         "(update_halo, advect3d_eq_cal_tend_dev with VMapM/VMapP gathers, "
                         "rk_stage_dev, OPT1 order) as the reference's loop calls them",
             "gdof_updates_per_s": rate, "ms_per_step": 1e3 * t / k, "steps": k,
-            "launches_per_step": 13, "fused_over_dropin": fused_rate / rate}
+            "launches_per_step": 13, "fused_over_dropin": fused_rate / rate,
+            "bytes_per_dof_update_with_geometry": bpd,
+            "achieved_gbs_with_geometry": bpd * rate}
 
 
 def bench_serving(sdg, args, rate=None):
