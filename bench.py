@@ -267,6 +267,10 @@ def roofline(precision, p, ne, ndof, t, steps, peaks, opt="opt1"):
     tkey = f"stage_{precision}_p{p}_ne{ne}"
     if precision == "fp64" and opt == "evenodd":
         kernel, tkey = f"stage_eo_kernel<{p}>", f"stage_fp64eo_p{p}_ne{ne}"
+    elif precision == "fp64emu" and opt == "evenodd":
+        kernel, tkey = f"stage_emu_eo_kernel<{p}>", f"stage_fp64emueo_p{p}_ne{ne}"
+    elif precision == "fp32" and opt == "evenodd":
+        kernel, tkey = f"stage_eo_kernel<{p},float>", f"stage_fp32eo_p{p}_ne{ne}"
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak,
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
@@ -394,6 +398,7 @@ def bench_order_sweep(sdg, args):
         for name, prec, opt in (("fp64", sdg.PREC_FP64, sdg.OPT_OPT1),
                                 ("fp64eo", sdg.PREC_FP64, sdg.OPT_EVENODD),
                                 ("fp64emu", sdg.PREC_FP64_EMU, sdg.OPT_OPT1),
+                                ("fp64emueo", sdg.PREC_FP64_EMU, sdg.OPT_EVENODD),
                                 ("fp32", sdg.PREC_FP32, sdg.OPT_OPT1),
                                 ("fp32eo", sdg.PREC_FP32, sdg.OPT_EVENODD)):
             s = sdg.Solver(ne, ne, ne, p, D, L, opt=opt, precision=prec)
@@ -404,7 +409,7 @@ def bench_order_sweep(sdg, args):
             row[f"{name}_gdof_updates_per_s"] = ndof * 3 * args.sweep_steps / (ms / 1e3) / 1e9
             row[f"{name}_mass_drift"] = abs(W.mass(res[name], x, ne, ne, ne) - m0) / abs(m0)
         ref = res["fp64"]
-        for name in ("fp64eo", "fp64emu", "fp32", "fp32eo"):
+        for name in ("fp64eo", "fp64emu", "fp64emueo", "fp32", "fp32eo"):
             row[f"{name}_rel_l2_vs_fp64"] = float(np.linalg.norm(res[name] - ref) /
                                                   np.linalg.norm(ref))
         out.append(row)
@@ -642,14 +647,14 @@ def run_ours(args, ws, rank, local):
     other = None
     if args.precision == "fp64" and not args.no_emu:
         se, te_, _ = time_solver(sdg, wl, p, ne, PRECISIONS["fp64emu"], args.steps,
-                                 args.warmup, local, barrier, False)
+                                 args.warmup, local, barrier, False, OPTS[args.opt])
         te_ = tmax(te_)
         other = {"precision": "fp64emu",
                  "description": "FP64 state and RK combine; flux, divergence and lift in "
                                 "double-float (two FP32 numbers) on the FP32 pipes",
                  "value": ws * ndof * 3 * args.steps / te_ / 1e9, "unit": "GDOF-updates/s",
                  "ms_per_step": 1e3 * te_ / args.steps,
-                 "roofline": roofline("fp64emu", p, ne, ndof, te_, args.steps, peaks)}
+                 "roofline": roofline("fp64emu", p, ne, ndof, te_, args.steps, peaks, args.opt)}
         tend_emu = None
         if rank == 0 and not args.no_cpu_baseline:
             se.upload(wl["q"], wl["u"], wl["v"], wl["w"])

@@ -53,9 +53,9 @@ extern "C" {
 #define SDG_OPT_OPT1 2
 /* Solver and batched forms only: the stage with the even-odd factorisation
  * of D1D and of the face lift (needs their centro-symmetry, which GLL
- * operators have to rounding); ~30 % fewer FP64 operations in the FP64 form
- * and far fewer shared-memory reads in the FP32 form, same result to
- * rounding.  The emulated form runs its own body for every opt type. */
+ * operators have to rounding); ~30 % fewer FP64 operations in the FP64 form,
+ * about half the instructions in the FP32 and emulated forms, same result to
+ * rounding. */
 #define SDG_OPT_EVENODD 3
 
 /* Arithmetic of a solver (the reference is FP64 throughout). */

@@ -190,6 +190,38 @@ void operator_tables(int prec, int Nq, const Box& box, const double* D1D,
   }
 }
 
+// Tables of the emulated even-odd stage (sdg_stage_emu_eo.cuh) as
+// double-float pairs, per axis: the even-odd tables `eo` (unscaled, from
+// eo_tables) with the D parts times -Es_d and the lift parts times
+// -0.5*Fs_d, then the row sums R(i), i < N/2, of the symmetrised operator
+// (long double) times -Es_d.
+void emu_eo_tables(int Nq, const Box& box, const double* D1D, const std::vector<double>& eo,
+                   std::vector<unsigned char>& out) {
+  const int N = Nq, H = N / 2, HR = (N + 1) / 2, ODD = N & 1;
+  const int TE = H * H + HR * H + ODD * H + HR + H, TE2 = TE + H;
+  const int offA = H * H + HR * H + ODD * H;
+  std::vector<float> f(2 * 3 * (size_t)TE2);
+  for (int ax = 0; ax < 3; ax++) {
+    const long double sD = -(long double)box.Es[ax];
+    const long double sL = -0.5L * (long double)box.Fs[ax];
+    auto put = [&](int w, long double v) {
+      const dfl x = df_from_double((double)v);
+      f[2 * ((size_t)ax * TE2 + w)] = x.hi;
+      f[2 * ((size_t)ax * TE2 + w) + 1] = x.lo;
+    };
+    for (int w = 0; w < TE; w++)
+      put(w, (long double)eo[(size_t)ax * TE + w] * (w < offA ? sD : sL));
+    for (int i = 0; i < H; i++) {
+      long double rs = 0.0L;
+      for (int l = 0; l < N; l++)
+        rs += 0.5L * ((long double)D1D[i + l * N] - (long double)D1D[(N - 1 - i) + (N - 1 - l) * N]);
+      put(TE + i, rs * sD);
+    }
+  }
+  out.resize(4 * f.size());
+  std::memcpy(out.data(), f.data(), out.size());
+}
+
 }  // namespace
 
 extern "C" {
@@ -230,14 +262,16 @@ int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
   // operator tables as the kernels read them (see operator_tables below)
   std::vector<unsigned char> dtab, ltab;
   operator_tables(precision, s->Nq, s->box, D1D, Lift_mat, dtab, ltab);
-  if (opt == SDG_OPT_EVENODD && precision != SDG_PREC_FP64_EMU) {
+  if (opt == SDG_OPT_EVENODD) {
     std::vector<double> tab;
     const int rc = eo_tables(s->Nq, D1D, Lift_mat, tab);
     if (rc != SDG_OK) {
       delete s;
       return rc;
     }
-    if (precision == SDG_PREC_FP32) {
+    if (precision == SDG_PREC_FP64_EMU) {
+      emu_eo_tables(s->Nq, s->box, D1D, tab, dtab);
+    } else if (precision == SDG_PREC_FP32) {
       // the FP32 form reads FP32 tables
       std::vector<float> f(tab.begin(), tab.end());
       dtab.resize(4 * f.size());

@@ -1,0 +1,313 @@
+// Emulated-FP64 stage with the even-odd factorisation (SDG_PREC_FP64_EMU with
+// SDG_OPT_EVENODD): the accuracy scheme of stage_emu_kernel (FP64
+// differences, double-float sums) on the pair structure of stage_eo_block.
+//
+// Per line of an axis d, with the line base F0 = q u_d at the line's node 0
+// and the differences G(l) = q u_d - F0 formed by one FP64 FMA (exact product
+// minus the base, rounded once), the pair values
+//     S(l) = G(l) + G(N-1-l),   Δ(l) = G(l) - G(N-1-l)      (l < N/2, FP64)
+// are split to double-float, and
+//     e_i = Σ_l E(i,l) S(l) + R(i) F0 [+ D(i,mid) G(mid)] + B(i) gd,
+//     o_i = Σ_l O(i,l) Δ(l) + A(i) gs,
+//     out(i) = e_i + o_i,  out(N-1-i) = o_i - e_i,
+// with compensated (Dot2) double-float sums.  R is the row sum of the
+// symmetrised FP64 operator, antisymmetric in i, so the base term joins e.
+// The tables carry -Escale (D part) and -0.5*Fscale (lift part), so the three
+// line results sum to dqdt; the RK update runs in FP64 as in stage_emu_kernel.
+//
+// A line now costs about N/2 + 2 compensated products per output instead of
+// N + 1 (plus the lift, which joins the same pairs), so the kernel issues
+// about half the instructions of stage_emu_kernel.
+//
+// Shared memory per element: three planes of double-float pair values, one
+// per axis, each line-major with a pad slot per line (the x plane then holds
+// the running compensated sums), the line bases, the face fluxes and the
+// neighbour indices.
+#pragma once
+
+#include "sdg_df.cuh"
+#include "sdg_stage.cuh"
+#include "sdg_stage_eo.cuh"
+
+namespace sdg {
+
+template <int P>
+struct EmuEoCfg {
+  static constexpr int NQ2 = (P + 1) * (P + 1);
+  static constexpr int EPB = (256 / NQ2) > 0 ? (256 / NQ2) : 1;
+  static constexpr int LINES = EPB * NQ2;
+  static constexpr int THREADS = ((LINES + 31) / 32) * 32;
+  static constexpr int PADL = P + 2;        // slots per line (N + 1)
+  static constexpr int PLANE = PADL * NQ2;  // slots per plane
+  static constexpr int TE = EoShape<P>::TE + EoShape<P>::H;  // + R(i), i < H
+  static constexpr int OFF_R = EoShape<P>::TE;
+};
+
+// Device table (float2 = hi, lo), per axis x, y, z: E, O, D(i,mid), A, B as in
+// EoShape (D parts times -Es_d, lift parts times -0.5*Fs_d), then R(i) times
+// -Es_d for i < N/2.
+template <int P>
+constexpr size_t emu_eo_smem_bytes() {
+  using C = EmuEoCfg<P>;
+  constexpr int NQ = P + 1, NQ2 = NQ * NQ, NFT = 6 * NQ2;
+  return 8 * (size_t)(3 * C::TE) +
+         (size_t)C::EPB * (8 * 3 * C::PLANE + 8 * 3 * NQ2 + 8 * NFT + 4 * 8);
+}
+
+__device__ __forceinline__ dacc dacc_of(dfl a) {
+  dacc r;
+  r.s = a.hi;
+  r.c = a.lo;
+  return r;
+}
+
+// o + e (MINUS = false) or o - e (MINUS = true) of two compensated sums.
+template <bool MINUS>
+__device__ __forceinline__ dacc dacc_combine(const dacc& o, const dacc& e) {
+  const float es = MINUS ? -e.s : e.s, ec = MINUS ? -e.c : e.c;
+  const dfl t = two_sum(o.s, es);
+  dacc r;
+  r.s = t.hi;
+  r.c = DFA(DFA(o.c, ec), t.lo);
+  return r;
+}
+
+// acc += x
+__device__ __forceinline__ void dacc_accum(dacc& acc, const dacc& x) {
+  const dfl t = two_sum(acc.s, x.s);
+  acc.s = t.hi;
+  acc.c = DFA(acc.c, DFA(x.c, t.lo));
+}
+
+__device__ __forceinline__ dfl f2_df(float2 v) { return df_make(v.x, v.y); }
+
+// One line of axis tables T: pair values (S at l, Δ at N-1-l, G(mid) at H) in
+// the row `row`, base b0, face fluxes gm / gp.  emit(m, sum) receives the
+// compensated result for position m, after all reads of the row.
+template <int P, typename Emit>
+__device__ __forceinline__ void emu_eo_line(const float2* row, const float2* __restrict__ T,
+                                            dfl b0, dfl gm, dfl gp, Emit&& emit) {
+  using Sh = EoShape<P>;
+  using C = EmuEoCfg<P>;
+  constexpr int N = Sh::N, H = Sh::H;
+  dfl s[H], d[H];
+#pragma unroll
+  for (int l = 0; l < H; l++) {
+    s[l] = f2_df(row[l]);
+    d[l] = f2_df(row[N - 1 - l]);
+  }
+  dfl gmid = df_make(0.f, 0.f);
+  if constexpr (Sh::ODD != 0) gmid = f2_df(row[H]);
+  const dfl gs = df_add(gm, gp), gd = df_sub(gm, gp);
+#pragma unroll 1
+  for (int i = 0; i < H; i++) {
+    dacc e = dacc_zero();
+#pragma unroll
+    for (int l = 0; l < H; l++) dacc_fma(e, f2_df(T[Sh::OFF_E + i * H + l]), s[l]);
+    dacc_fma(e, f2_df(T[C::OFF_R + i]), b0);
+    if constexpr (Sh::ODD != 0) dacc_fma(e, f2_df(T[Sh::OFF_DM + i]), gmid);
+    dacc_fma(e, f2_df(T[Sh::OFF_B + i]), gd);
+    dacc o = dacc_zero();
+#pragma unroll
+    for (int l = 0; l < H; l++) dacc_fma(o, f2_df(T[Sh::OFF_O + i * H + l]), d[l]);
+    dacc_fma(o, f2_df(T[Sh::OFF_A + i]), gs);
+    emit(i, dacc_combine<false>(o, e));
+    emit(N - 1 - i, dacc_combine<true>(o, e));
+  }
+  if constexpr (Sh::ODD != 0) {
+    dacc o = dacc_zero();
+#pragma unroll
+    for (int l = 0; l < H; l++) dacc_fma(o, f2_df(T[Sh::OFF_O + H * H + l]), d[l]);
+    dacc_fma(o, f2_df(T[Sh::OFF_A + H]), gs);
+    emit(H, o);
+  }
+}
+
+template <int P>
+__global__ void __launch_bounds__(EmuEoCfg<P>::THREADS) stage_emu_eo_kernel(const StageArgs a) {
+  using O = Ord<P>;
+  using Sh = EoShape<P>;
+  using C = EmuEoCfg<P>;
+  constexpr int NQ = O::NQ, NQ2 = O::NQ2, NP = O::NP, NFP = O::NFP, NFT = O::NFT,
+                EPB = C::EPB, PADL = C::PADL, PLANE = C::PLANE, TE = C::TE, H = Sh::H,
+                HR = Sh::HR;
+  const int T = blockDim.x;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* sT = reinterpret_cast<float2*>(smem_raw);                // [3][TE]
+  float2* sPl = sT + 3 * TE;                                       // [EPB][3][PLANE]
+  double* sF0 = reinterpret_cast<double*>(sPl + EPB * 3 * PLANE);  // [EPB][3][NQ2]
+  float2* sg = reinterpret_cast<float2*>(sF0 + EPB * 3 * NQ2);     // [EPB][NFT]
+  int* snb = reinterpret_cast<int*>(sg + EPB * NFT);               // [EPB][8]
+
+  const long long eb = a.elem_begin + (long long)blockIdx.x * EPB;
+  const long long eend = a.elem_begin + a.elem_count;
+  const int nloc = (int)((eend - eb) < EPB ? (eend - eb) : EPB);
+  if (nloc <= 0) return;
+  const double* __restrict__ qin = a.q_in;
+  const double* __restrict__ gu = static_cast<const double*>(a.u);
+  const double* __restrict__ gv = static_cast<const double*>(a.v);
+  const double* __restrict__ gw = static_cast<const double*>(a.w);
+  const long long g0 = eb * NP;
+
+  // node of line r of axis d at position c along the axis
+  auto line_node = [](int d, int r, int c) -> int {
+    return (d == 0) ? c + NQ * r : (d == 1) ? (r % NQ) + NQ * c + NQ2 * (r / NQ) : r + NQ2 * c;
+  };
+
+  // phase 0: tables, neighbour elements, line bases F0 = q u_d at node 0
+  {
+    const float2* tab = static_cast<const float2*>(a.D);
+    for (int t = threadIdx.x; t < 3 * TE; t += T) sT[t] = tab[t];
+  }
+  for (int t = threadIdx.x; t < 6 * nloc; t += T)
+    snb[8 * (t / 6) + t % 6] = (int)neighbor(a.box, eb + t / 6, t % 6);
+  for (int t = threadIdx.x; t < nloc * 3 * NQ2; t += T) {
+    const int le = t / (3 * NQ2);
+    const int rr = t - le * 3 * NQ2;
+    const int d = rr / NQ2, r = rr - d * NQ2;
+    const long long g = g0 + (long long)le * NP + line_node(d, r, 0);
+    const double* gvel = (d == 0) ? gu : (d == 1) ? gv : gw;
+    sF0[t] = qin[g] * gvel[g];
+  }
+  __syncthreads();
+
+  // phase 1a: face fluxes g = qP (VP - VM) + (qP - qM)(VM - alpha), as
+  // stage_emu_kernel forms them
+  for (int t = threadIdx.x; t < nloc * NFT; t += T) {
+    const int le = t / NFT;
+    const int r = t - le * NFT;
+    const int f = r / NFP;
+    const int fp = r - f * NFP;
+    int nM, nP, axis, sgi;
+    face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sgi);
+    const long long gM = g0 + (long long)le * NP + nM;
+    const long long gP = (long long)snb[8 * le + f] * NP + nP;
+    const double* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
+    const double qM = qin[gM], qP = qin[gP];
+    const double VM = (sgi > 0) ? gvel[gM] : -gvel[gM];
+    const double VP = (sgi > 0) ? gvel[gP] : -gvel[gP];
+    const double jq = qP - qM, jV = VP - VM;  // FP64 jumps
+    const dfl dVM = df_split(VM);
+    const dfl alpha = df_scale2(df_abs(df_add(df_split(VP), dVM)), 0.5f);
+    dacc A = dacc_zero();
+    dacc_fma(A, df_split(qP), df_split(jV));
+    dacc_fma(A, df_split(jq), df_sub(dVM, alpha));
+    const dfl gf = dacc_result(A);
+    sg[t] = make_float2(gf.hi, gf.lo);
+  }
+  // phase 1b: pair values per (axis, line, c < ceil(N/2)): the differences
+  // G = q u_d - F0 by one FMA each, then S and Δ in FP64, split
+  for (int t = threadIdx.x; t < nloc * 3 * HR * NQ2; t += T) {
+    const int le = t / (3 * HR * NQ2);
+    const int rr = t - le * 3 * HR * NQ2;
+    const int d = rr / (HR * NQ2);
+    const int w = rr - d * HR * NQ2;
+    const int c = w / NQ2, r = w - c * NQ2;
+    const double* gvel = (d == 0) ? gu : (d == 1) ? gv : gw;
+    const long long ge = g0 + (long long)le * NP;
+    const double f0 = sF0[le * 3 * NQ2 + d * NQ2 + r];
+    float2* row = sPl + (le * 3 + d) * PLANE + r * PADL;
+    const int n = line_node(d, r, c);
+    const double G1 = fma(qin[ge + n], gvel[ge + n], -f0);
+    if (c < H) {
+      const int n2 = line_node(d, r, NQ - 1 - c);
+      const double G2 = fma(qin[ge + n2], gvel[ge + n2], -f0);
+      const dfl S = df_split(G1 + G2), D = df_split(G1 - G2);
+      row[c] = make_float2(S.hi, S.lo);
+      row[NQ - 1 - c] = make_float2(D.hi, D.lo);
+    } else {
+      const dfl M = df_split(G1);
+      row[c] = make_float2(M.hi, M.lo);
+    }
+  }
+  __syncthreads();
+
+  // line phases: one thread per line; the x plane then holds the running
+  // compensated sums of the nodes, at the node's x-line slot
+  const int r = threadIdx.x - (threadIdx.x / NQ2) * NQ2;
+  const int le = threadIdx.x / NQ2;
+  const bool has_line = le < nloc;
+  float2* xpl = sPl + le * 3 * PLANE;
+  const float2* gl = sg + le * NFT;
+
+  // x lines: r = j + k N; faces -x (3), +x (1) at face node r
+  if (has_line) {
+    const dfl b0 = df_split(sF0[le * 3 * NQ2 + r]);
+    float2* row = xpl + r * PADL;
+    emu_eo_line<P>(row, sT, b0, f2_df(gl[3 * NFP + r]), f2_df(gl[1 * NFP + r]),
+                   [&](int m, const dacc& v) { row[m] = make_float2(v.s, v.c); });
+  }
+  __syncthreads();
+
+  // y lines: r = i + k N; faces -y (0), +y (2); node (i, m, k) sits in x-line
+  // m + k N at slot i
+  if (has_line) {
+    const int i = r % NQ, k = r / NQ;
+    const dfl b0 = df_split(sF0[le * 3 * NQ2 + NQ2 + r]);
+    emu_eo_line<P>(xpl + PLANE + r * PADL, sT + TE, b0, f2_df(gl[r]), f2_df(gl[2 * NFP + r]),
+                   [&](int m, const dacc& v) {
+                     float2* s = xpl + (m + k * NQ) * PADL + i;
+                     dacc acc;
+                     acc.s = s->x;
+                     acc.c = s->y;
+                     dacc_accum(acc, v);
+                     *s = make_float2(acc.s, acc.c);
+                   });
+  }
+  __syncthreads();
+
+  // z lines: r = i + j N; faces -z (4), +z (5); finish and RK update
+  if (has_line) {
+    const int i = r % NQ, j = r / NQ;
+    const dfl b0 = df_split(sF0[le * 3 * NQ2 + 2 * NQ2 + r]);
+    const dfl c_dt = df_make(a.cdt_hi, a.cdt_lo);
+    double* __restrict__ qout = a.q_out;
+    const double* __restrict__ q0 = a.q0;
+    const double ra = a.a, rb = a.b;
+    const long long ge = g0 + (long long)le * NP;
+    with_rk_kind(rk_kind(a), [&](auto rkc) {
+      constexpr int RK = decltype(rkc)::value;
+      emu_eo_line<P>(xpl + 2 * PLANE + r * PADL, sT + 2 * TE, b0, f2_df(gl[4 * NFP + r]),
+                     f2_df(gl[5 * NFP + r]), [&](int m, const dacc& v) {
+                       const float2 s = xpl[(j + m * NQ) * PADL + i];
+                       dacc acc;
+                       acc.s = s.x;
+                       acc.c = s.y;
+                       dacc_accum(acc, v);
+                       const dfl dq = dacc_result(acc);
+                       const long long g = ge + i + j * NQ + m * NQ2;
+                       if constexpr (RK == kRkTend) {
+                         qout[g] = f32_to_f64_bits(dq.hi) + f32_to_f64_bits(dq.lo);
+                       } else {
+                         const dfl inc = df_mul(c_dt, dq);  // (b*dt)*dqdt
+                         const double ih = f32_to_f64_bits(inc.hi), il = f32_to_f64_bits(inc.lo);
+                         const double qv = qin[g];
+                         if constexpr (RK == kRkFirst)
+                           qout[g] = (qv + ih) + il;
+                         else
+                           qout[g] = fma(ra, q0[g], fma(rb, qv, ih) + il);
+                       }
+                     });
+    });
+  }
+}
+
+template <int P>
+int launch_stage_emu_eo_impl(const StageArgs& a, cudaStream_t st) {
+  using C = EmuEoCfg<P>;
+  constexpr size_t smem = emu_eo_smem_bytes<P>();
+  static bool attr_done = false;
+  if (!attr_done) {
+    SDG_CUDA_TRY(cudaFuncSetAttribute(stage_emu_eo_kernel<P>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_done = true;
+  }
+  const long long nblk = (a.elem_count + C::EPB - 1) / C::EPB;
+  if (nblk <= 0) return SDG_OK;
+  if (nblk > 0x7fffffffLL) return fail(SDG_ERR_INVALID_ARG, "too many elements");
+  stage_emu_eo_kernel<P><<<(unsigned)nblk, C::THREADS, smem, st>>>(a);
+  SDG_CUDA_TRY(cudaGetLastError());
+  return SDG_OK;
+}
+
+}  // namespace sdg

@@ -4,6 +4,7 @@
 
 #include "sdg_stage.cuh"
 #include "sdg_stage_emu.cuh"
+#include "sdg_stage_emu_eo.cuh"
 #include "sdg_stage_eo.cuh"
 
 namespace sdg {
@@ -11,10 +12,12 @@ namespace sdg {
 template <int P>
 int launch_stage_order(int prec, int opt, const StageArgs& a, cudaStream_t st) {
   constexpr bool kCanSplit = (P > 7);
-  // EVENODD: the even-odd bodies (FP64 and FP32); the emulated form runs its
-  // own line body for every opt type
+  // EVENODD: the even-odd bodies (FP64, FP32 and emulated FP64)
   const bool split = kCanSplit && (opt != SDG_OPT_GENERAL);
-  if (prec == SDG_PREC_FP64_EMU) return launch_stage_emu_impl<P>(a, st);
+  if (prec == SDG_PREC_FP64_EMU) {
+    if (opt == SDG_OPT_EVENODD) return launch_stage_emu_eo_impl<P>(a, st);
+    return launch_stage_emu_impl<P>(a, st);
+  }
   if (opt == SDG_OPT_EVENODD) {
     if (prec == SDG_PREC_FP64) return launch_stage_eo_impl<P, double>(a, st);
     return launch_stage_eo_impl<P, float>(a, st);

@@ -46,6 +46,7 @@ def test_fused_stage_tendency_matches_oracle(p, opt):
                                           (sdg.OPT_GENERAL, sdg.PREC_FP64, TOL_TEND),
                                           (sdg.OPT_EVENODD, sdg.PREC_FP64, TOL_TEND),
                                           (sdg.OPT_OPT1, sdg.PREC_FP64_EMU, TOL_TEND),
+                                          (sdg.OPT_EVENODD, sdg.PREC_FP64_EMU, TOL_TEND),
                                           (sdg.OPT_OPT1, sdg.PREC_FP32, TOL_FP32),
                                           (sdg.OPT_EVENODD, sdg.PREC_FP32, TOL_FP32)])
 def test_single_element_box_is_its_own_neighbour(p, opt, prec, tol):
@@ -101,10 +102,12 @@ def test_evenodd_refuses_operators_without_centro_symmetry():
 
 @pytest.mark.parametrize("p", range(1, 16))
 @pytest.mark.parametrize("ic", ["blob", "sine"])
-def test_emulated_fp64_tendency_matches_oracle(p, ic):
-    """Double-float arithmetic on the FP32 pipes meets the FP64 tolerance."""
+@pytest.mark.parametrize("opt", [sdg.OPT_OPT1, sdg.OPT_EVENODD])
+def test_emulated_fp64_tendency_matches_oracle(p, ic, opt):
+    """Double-float arithmetic on the FP32 pipes meets the FP64 tolerance, in
+    the line body and in the even-odd body."""
     c = Case(*mesh_dims(p), p, ic=ic)
-    s = solver_for(c, prec=sdg.PREC_FP64_EMU)
+    s = solver_for(c, opt=opt, prec=sdg.PREC_FP64_EMU)
     assert rel_l2(s.tendency(), c.oracle_tend()) <= TOL_TEND
 
 
@@ -114,10 +117,12 @@ def test_emulated_fp64_tendency_matches_oracle(p, ic):
     (10, (2, 2, 2), 5, "blob"),
     (1, (1, 2, 3), 30, "blob"),       # elements that are their own x-neighbour
 ])
-@pytest.mark.parametrize("prec", [sdg.PREC_FP64, sdg.PREC_FP64_EMU])
-def test_solver_run_matches_oracle(p, dims, nstep, ic, prec):
+@pytest.mark.parametrize("prec,opt", [(sdg.PREC_FP64, sdg.OPT_OPT1),
+                                      (sdg.PREC_FP64_EMU, sdg.OPT_OPT1),
+                                      (sdg.PREC_FP64_EMU, sdg.OPT_EVENODD)])
+def test_solver_run_matches_oracle(p, dims, nstep, ic, prec, opt):
     c = Case(*dims, p, ic=ic)
-    s = solver_for(c, prec=prec)
+    s = solver_for(c, opt=opt, prec=prec)
     s.step(c.dt, nstep)
     q = s.download()
     assert rel_l2(q, c.oracle_run(nstep)) <= TOL_RUN
@@ -478,7 +483,8 @@ def full_case():
 
 @pytest.mark.parametrize("prec,opt", [(sdg.PREC_FP64, sdg.OPT_OPT1),
                                       (sdg.PREC_FP64_EMU, sdg.OPT_OPT1),
-                                      (sdg.PREC_FP64, sdg.OPT_EVENODD)])
+                                      (sdg.PREC_FP64, sdg.OPT_EVENODD),
+                                      (sdg.PREC_FP64_EMU, sdg.OPT_EVENODD)])
 def test_full_size_tendency_matches_oracle(full_case, prec, opt):
     f = full_case
     N, p = f["N"], f["p"]
@@ -495,7 +501,8 @@ def test_full_size_tendency_matches_oracle(full_case, prec, opt):
 
 @pytest.mark.parametrize("prec,opt", [(sdg.PREC_FP64, sdg.OPT_OPT1),
                                       (sdg.PREC_FP64_EMU, sdg.OPT_OPT1),
-                                      (sdg.PREC_FP64, sdg.OPT_EVENODD)])
+                                      (sdg.PREC_FP64, sdg.OPT_EVENODD),
+                                      (sdg.PREC_FP64_EMU, sdg.OPT_EVENODD)])
 def test_full_size_mass_conservation_and_shift_invariance(full_case, prec, opt):
     f = full_case
     N, p, Np = f["N"], f["p"], (f["p"] + 1) ** 3
