@@ -15,14 +15,15 @@
 // The tables carry -Escale (D part) and -0.5*Fscale (lift part), so the three
 // line results sum to dqdt; the RK update runs in FP64 as in stage_emu_kernel.
 //
-// A line now costs about N/2 + 2 compensated products per output instead of
-// N + 1 (plus the lift, which joins the same pairs), so the kernel issues
-// about half the instructions of stage_emu_kernel.
+// A line costs about N/2 + 2 compensated products per output instead of
+// N + 1 (plus the lift, which joins the same pairs).
 //
-// Shared memory per element: three planes of double-float pair values, one
-// per axis, each line-major with a pad slot per line (the x plane then holds
-// the running compensated sums), the line bases, the face fluxes and the
-// neighbour indices.
+// Shared memory per element: one plane of double-float values, line-major for
+// the x axis with a pad slot per line (first the x pair values, then the
+// running compensated sums of the nodes), the x line bases, the face fluxes
+// and the neighbour indices.  The y and z pair values are formed by the line
+// threads of those phases from q and v / w in global memory (cached), which
+// keeps the footprint at a third and lets four blocks share an SM.
 #pragma once
 
 #include "sdg_df.cuh"
@@ -51,7 +52,32 @@ constexpr size_t emu_eo_smem_bytes() {
   using C = EmuEoCfg<P>;
   constexpr int NQ = P + 1, NQ2 = NQ * NQ, NFT = 6 * NQ2;
   return 8 * (size_t)(3 * C::TE) +
-         (size_t)C::EPB * (8 * 3 * C::PLANE + 8 * 3 * NQ2 + 8 * NFT + 4 * 8);
+         (size_t)C::EPB * (8 * C::PLANE + 8 * NQ2 + 8 * NFT + 4 * 8);
+}
+
+// Pair values of one line from global memory: F0 = q u at the line's node 0,
+// G = q u - F0 by one FMA, S and Δ in FP64, split; written to row[0..N).
+template <int P>
+__device__ __forceinline__ void emu_eo_pairs(const double* __restrict__ q,
+                                             const double* __restrict__ vel, long long g0,
+                                             int stride, float2* row, double& f0) {
+  using Sh = EoShape<P>;
+  constexpr int N = Sh::N, H = Sh::H;
+  f0 = q[g0] * vel[g0];
+#pragma unroll
+  for (int c = 0; c < H; c++) {
+    const long long a = g0 + (long long)c * stride, b = g0 + (long long)(N - 1 - c) * stride;
+    const double G1 = fma(q[a], vel[a], -f0);
+    const double G2 = fma(q[b], vel[b], -f0);
+    const dfl S = df_split(G1 + G2), D = df_split(G1 - G2);
+    row[c] = make_float2(S.hi, S.lo);
+    row[N - 1 - c] = make_float2(D.hi, D.lo);
+  }
+  if constexpr (Sh::ODD != 0) {
+    const long long a = g0 + (long long)H * stride;
+    const dfl M = df_split(fma(q[a], vel[a], -f0));
+    row[H] = make_float2(M.hi, M.lo);
+  }
 }
 
 __device__ __forceinline__ dacc dacc_of(dfl a) {
@@ -124,7 +150,8 @@ __device__ __forceinline__ void emu_eo_line(const float2* row, const float2* __r
 }
 
 template <int P>
-__global__ void __launch_bounds__(EmuEoCfg<P>::THREADS) stage_emu_eo_kernel(const StageArgs a) {
+__global__ void __launch_bounds__(EmuEoCfg<P>::THREADS, 4)
+    stage_emu_eo_kernel(const StageArgs a) {
   using O = Ord<P>;
   using Sh = EoShape<P>;
   using C = EmuEoCfg<P>;
@@ -133,11 +160,11 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS) stage_emu_eo_kernel(cons
                 HR = Sh::HR;
   const int T = blockDim.x;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* sT = reinterpret_cast<float2*>(smem_raw);                // [3][TE]
-  float2* sPl = sT + 3 * TE;                                       // [EPB][3][PLANE]
-  double* sF0 = reinterpret_cast<double*>(sPl + EPB * 3 * PLANE);  // [EPB][3][NQ2]
-  float2* sg = reinterpret_cast<float2*>(sF0 + EPB * 3 * NQ2);     // [EPB][NFT]
-  int* snb = reinterpret_cast<int*>(sg + EPB * NFT);               // [EPB][8]
+  float2* sT = reinterpret_cast<float2*>(smem_raw);            // [3][TE]
+  float2* sPl = sT + 3 * TE;                                   // [EPB][PLANE]
+  double* sF0 = reinterpret_cast<double*>(sPl + EPB * PLANE);  // [EPB][NQ2], x lines
+  float2* sg = reinterpret_cast<float2*>(sF0 + EPB * NQ2);     // [EPB][NFT]
+  int* snb = reinterpret_cast<int*>(sg + EPB * NFT);           // [EPB][8]
 
   const long long eb = a.elem_begin + (long long)blockIdx.x * EPB;
   const long long eend = a.elem_begin + a.elem_count;
@@ -161,13 +188,10 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS) stage_emu_eo_kernel(cons
   }
   for (int t = threadIdx.x; t < 6 * nloc; t += T)
     snb[8 * (t / 6) + t % 6] = (int)neighbor(a.box, eb + t / 6, t % 6);
-  for (int t = threadIdx.x; t < nloc * 3 * NQ2; t += T) {
-    const int le = t / (3 * NQ2);
-    const int rr = t - le * 3 * NQ2;
-    const int d = rr / NQ2, r = rr - d * NQ2;
-    const long long g = g0 + (long long)le * NP + line_node(d, r, 0);
-    const double* gvel = (d == 0) ? gu : (d == 1) ? gv : gw;
-    sF0[t] = qin[g] * gvel[g];
+  for (int t = threadIdx.x; t < nloc * NQ2; t += T) {
+    const int le = t / NQ2, r = t - le * NQ2;
+    const long long g = g0 + (long long)le * NP + line_node(0, r, 0);
+    sF0[t] = qin[g] * gu[g];
   }
   __syncthreads();
 
@@ -195,18 +219,17 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS) stage_emu_eo_kernel(cons
     const dfl gf = dacc_result(A);
     sg[t] = make_float2(gf.hi, gf.lo);
   }
-  // phase 1b: pair values per (axis, line, c < ceil(N/2)): the differences
-  // G = q u_d - F0 by one FMA each, then S and Δ in FP64, split
-  for (int t = threadIdx.x; t < nloc * 3 * HR * NQ2; t += T) {
-    const int le = t / (3 * HR * NQ2);
-    const int rr = t - le * 3 * HR * NQ2;
-    const int d = rr / (HR * NQ2);
-    const int w = rr - d * HR * NQ2;
-    const int c = w / NQ2, r = w - c * NQ2;
-    const double* gvel = (d == 0) ? gu : (d == 1) ? gv : gw;
+  // phase 1b: x pair values per (line, c < ceil(N/2)): the differences
+  // G = q u - F0 by one FMA each, then S and Δ in FP64, split
+  for (int t = threadIdx.x; t < nloc * HR * NQ2; t += T) {
+    const int le = t / (HR * NQ2);
+    const int w = t - le * HR * NQ2;
+    const int c = w % HR, r = w / HR;  // c fastest: a warp reads whole lines
+    const double* gvel = gu;
     const long long ge = g0 + (long long)le * NP;
-    const double f0 = sF0[le * 3 * NQ2 + d * NQ2 + r];
-    float2* row = sPl + (le * 3 + d) * PLANE + r * PADL;
+    const double f0 = sF0[le * NQ2 + r];
+    float2* row = sPl + le * PLANE + r * PADL;
+    const int d = 0;
     const int n = line_node(d, r, c);
     const double G1 = fma(qin[ge + n], gvel[ge + n], -f0);
     if (c < H) {
@@ -227,12 +250,13 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS) stage_emu_eo_kernel(cons
   const int r = threadIdx.x - (threadIdx.x / NQ2) * NQ2;
   const int le = threadIdx.x / NQ2;
   const bool has_line = le < nloc;
-  float2* xpl = sPl + le * 3 * PLANE;
+  float2* xpl = sPl + le * PLANE;
   const float2* gl = sg + le * NFT;
+  const long long ge = g0 + (long long)le * NP;
 
   // x lines: r = j + k N; faces -x (3), +x (1) at face node r
   if (has_line) {
-    const dfl b0 = df_split(sF0[le * 3 * NQ2 + r]);
+    const dfl b0 = df_split(sF0[le * NQ2 + r]);
     float2* row = xpl + r * PADL;
     emu_eo_line<P>(row, sT, b0, f2_df(gl[3 * NFP + r]), f2_df(gl[1 * NFP + r]),
                    [&](int m, const dacc& v) { row[m] = make_float2(v.s, v.c); });
@@ -243,8 +267,11 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS) stage_emu_eo_kernel(cons
   // m + k N at slot i
   if (has_line) {
     const int i = r % NQ, k = r / NQ;
-    const dfl b0 = df_split(sF0[le * 3 * NQ2 + NQ2 + r]);
-    emu_eo_line<P>(xpl + PLANE + r * PADL, sT + TE, b0, f2_df(gl[r]), f2_df(gl[2 * NFP + r]),
+    float2 row[NQ];
+    double f0;
+    emu_eo_pairs<P>(qin, gv, ge + i + NQ2 * k, NQ, row, f0);
+    const dfl b0 = df_split(f0);
+    emu_eo_line<P>(row, sT + TE, b0, f2_df(gl[r]), f2_df(gl[2 * NFP + r]),
                    [&](int m, const dacc& v) {
                      float2* s = xpl + (m + k * NQ) * PADL + i;
                      dacc acc;
@@ -259,15 +286,17 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS) stage_emu_eo_kernel(cons
   // z lines: r = i + j N; faces -z (4), +z (5); finish and RK update
   if (has_line) {
     const int i = r % NQ, j = r / NQ;
-    const dfl b0 = df_split(sF0[le * 3 * NQ2 + 2 * NQ2 + r]);
+    float2 row[NQ];
+    double f0;
+    emu_eo_pairs<P>(qin, gw, ge + i + NQ * j, NQ2, row, f0);
+    const dfl b0 = df_split(f0);
     const dfl c_dt = df_make(a.cdt_hi, a.cdt_lo);
     double* __restrict__ qout = a.q_out;
     const double* __restrict__ q0 = a.q0;
     const double ra = a.a, rb = a.b;
-    const long long ge = g0 + (long long)le * NP;
     with_rk_kind(rk_kind(a), [&](auto rkc) {
       constexpr int RK = decltype(rkc)::value;
-      emu_eo_line<P>(xpl + 2 * PLANE + r * PADL, sT + 2 * TE, b0, f2_df(gl[4 * NFP + r]),
+      emu_eo_line<P>(row, sT + 2 * TE, b0, f2_df(gl[4 * NFP + r]),
                      f2_df(gl[5 * NFP + r]), [&](int m, const dacc& v) {
                        const float2 s = xpl[(j + m * NQ) * PADL + i];
                        dacc acc;
