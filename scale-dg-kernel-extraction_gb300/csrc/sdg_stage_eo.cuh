@@ -87,10 +87,14 @@ __host__ __device__ constexpr bool eo_stages_q() {
 
 // (The FP32 body keeps the line-result sums in their own array, since two
 // threads share a line and one may write before the other has read.)
+// The FP64 body keeps one array: the x lines' pair values, then the sums; the
+// y and z line threads form their lines' pair values from q and v / w in
+// cache.  That leaves room for four resident blocks.
 template <int P, typename CT>
 __host__ __device__ constexpr size_t eo_block_smem(int nloc) {
   using O = Ord<P>;
-  constexpr int arrays = (eo_stages_q<CT>() ? 4 : 3) + (eo_parts<CT>() > 1 ? 1 : 0);
+  constexpr int arrays =
+      sizeof(CT) == 8 ? 1 : (eo_stages_q<CT>() ? 4 : 3) + (eo_parts<CT>() > 1 ? 1 : 0);
   return sizeof(CT) * (size_t)(3 * EoShape<P>::TE + nloc * (arrays * O::NP + O::NFT)) +
          sizeof(int) * 6 * (size_t)nloc;
 }
@@ -106,7 +110,10 @@ __device__ __forceinline__ float abs_ct(float x) { return fabsf(x); }
 // With PARTS threads on a line, thread `part` produces the pairs of rows
 // [part * RPP, (part + 1) * RPP) (RPP = ceil(H / PARTS)) and the last part the
 // middle row of an odd N.
-template <int P, int S, int PARTS, typename CT, typename Emit>
+// PAIRED: F holds S(l) at l and Δ(l) at N-1-l (l < N/2) and, for odd N, F
+// at the middle, formed when the line was loaded; otherwise F holds the N
+// fluxes and the pair values are formed here.
+template <int P, int S, int PARTS, bool PAIRED, typename CT, typename Emit>
 __device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, CT gm, CT gp,
                                         int part, Emit&& emit) {
   using Sh = EoShape<P>;
@@ -116,8 +123,13 @@ __device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, C
 #pragma unroll
   for (int l = 0; l < H; l++) {
     const CT lo = F[l * S], hi = F[(N - 1 - l) * S];
-    s[l] = lo + hi;
-    d[l] = lo - hi;
+    if constexpr (PAIRED) {
+      s[l] = lo;
+      d[l] = hi;
+    } else {
+      s[l] = lo + hi;
+      d[l] = lo - hi;
+    }
   }
   CT fm = CT(0);
   if constexpr (Sh::ODD != 0) fm = F[H * S];
@@ -151,6 +163,26 @@ __device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, C
   }
 }
 
+// Pair values of one line from q and the axis velocity in global memory (FP64
+// body): S(c) = F(c) + F(N-1-c) and Δ(c) = F(c) - F(N-1-c) with F = q u, as
+// P' = q' u' and fma(q, u, ±P') -- three operations a pair instead of four.
+template <int P>
+__device__ __forceinline__ void eo_pairs_f64(const double* __restrict__ q,
+                                             const double* __restrict__ vel, long long g,
+                                             int stride, double* row) {
+  using Sh = EoShape<P>;
+  constexpr int N = Sh::N, H = Sh::H;
+#pragma unroll
+  for (int c = 0; c < H; c++) {
+    const long long a = g + (long long)c * stride, b = g + (long long)(N - 1 - c) * stride;
+    const double q1 = q[a], u1 = vel[a];
+    const double p2 = q[b] * vel[b];
+    row[c] = fma(q1, u1, p2);
+    row[N - 1 - c] = fma(q1, u1, -p2);
+  }
+  if constexpr (Sh::ODD != 0) row[H] = q[g + (long long)H * stride] * vel[g + (long long)H * stride];
+}
+
 // One block advances elements [eb, eb + nloc) through one stage with the
 // even-odd body.  CT = double: FP64 throughout (tables scaled by eo_sD /
 // eo_sL).  CT = float: the FP32-compute form (FP32 tables, velocity and
@@ -169,12 +201,12 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   CT* sT = reinterpret_cast<CT*>(smem);  // 3 directions x TE
   constexpr bool kSQ = eo_stages_q<CT>();
   CT* sq = sT + 3 * TE;      // q (FP32 body only)
-  CT* sFx = sq + (kSQ ? nloc * NP : 0);  // F_x, then the running sum of the line results
-  CT* sFy = sFx + nloc * NP;
-  CT* sFz = sFy + nloc * NP;
+  CT* sFx = sq + (kSQ ? nloc * NP : 0);  // F_x (FP64: x pair values), then the sums
+  CT* sFy = sFx + (kF64 ? 0 : nloc * NP);  // FP32 only
+  CT* sFz = sFy + (kF64 ? 0 : nloc * NP);  // FP32 only
   constexpr int PARTS = eo_parts<CT>();
   CT* sAcc = (PARTS > 1) ? sFz + nloc * NP : sFx;  // line-result sums
-  CT* sf = sFz + nloc * NP * (PARTS > 1 ? 2 : 1);
+  CT* sf = kF64 ? sFx + nloc * NP : sFz + nloc * NP * (PARTS > 1 ? 2 : 1);
   int* snb = reinterpret_cast<int*>(sf + nloc * NFT);
 
   const double* __restrict__ qin = a.q_in;
@@ -206,12 +238,31 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   }
   for (int t = threadIdx.x; t < 6 * nloc; t += T)
     snb[t] = (int)neighbor(a.box, eb + t / 6, t % 6);
-  for (int t = threadIdx.x; t < nloc * NP; t += T) {
-    const CT qq = to_ct<CT>(qin[g0 + t]);
-    if constexpr (kSQ) sq[t] = qq;
-    sFx[t] = qq * gu[g0 + t];
-    sFy[t] = qq * gv[g0 + t];
-    sFz[t] = qq * gw[g0 + t];
+  if constexpr (kF64) {
+    // x pair values: one task per (element, x line, c < ceil(N/2)), c fastest
+    constexpr int HR = Sh::HR, H = Sh::H;
+    for (int t = threadIdx.x; t < nloc * NQ2 * HR; t += T) {
+      const int le = t / (NQ2 * HR), w = t - le * NQ2 * HR;
+      const int r = w / HR, c = w - r * HR;
+      const long long g = g0 + (long long)le * NP + (long long)r * NQ;
+      CT* row = sFx + le * NP + r * NQ;
+      if (c < H) {
+        const double q1 = qin[g + c], u1 = gu[g + c];
+        const double p2 = qin[g + NQ - 1 - c] * gu[g + NQ - 1 - c];
+        row[c] = fma(q1, u1, p2);
+        row[NQ - 1 - c] = fma(q1, u1, -p2);
+      } else {
+        row[c] = qin[g + c] * gu[g + c];
+      }
+    }
+  } else {
+    for (int t = threadIdx.x; t < nloc * NP; t += T) {
+      const CT qq = to_ct<CT>(qin[g0 + t]);
+      if constexpr (kSQ) sq[t] = qq;
+      sFx[t] = qq * gu[g0 + t];
+      sFy[t] = qq * gv[g0 + t];
+      sFz[t] = qq * gw[g0 + t];
+    }
   }
   __syncthreads();
 
@@ -249,7 +300,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
     const CT* F = sFx + le * NP + r * NQ;
     CT* acc = sAcc + le * NP + r * NQ;
     const CT* fl = sf + le * NFT + r;
-    eo_line<P, 1, PARTS>(F, sT, fl[3 * NFP], fl[1 * NFP], part,
+    eo_line<P, 1, PARTS, kF64>(F, sT, fl[3 * NFP], fl[1 * NFP], part,
                          [&](int m, CT v) { acc[m] = v; });
   }
   __syncthreads();
@@ -261,8 +312,15 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
     const int off = le * NP + (r % NQ) + (r / NQ) * NQ2;
     CT* acc = sAcc + off;
     const CT* fl = sf + le * NFT + r;
-    eo_line<P, NQ, PARTS>(sFy + off, sT + TE, fl[0], fl[2 * NFP], part,
-                          [&](int m, CT v) { acc[m * NQ] += v; });
+    if constexpr (kF64) {
+      double row[NQ];
+      eo_pairs_f64<P>(qin, gv, g0 + off, NQ, row);
+      eo_line<P, 1, PARTS, true>(row, sT + TE, fl[0], fl[2 * NFP], part,
+                                 [&](int m, CT v) { acc[m * NQ] += v; });
+    } else {
+      eo_line<P, NQ, PARTS, false>(sFy + off, sT + TE, fl[0], fl[2 * NFP], part,
+                                   [&](int m, CT v) { acc[m * NQ] += v; });
+    }
   }
   __syncthreads();
 
@@ -280,8 +338,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
       const int le = lt / NQ2, r = lt - le * NQ2;
       const int off = le * NP + r;
       const CT* fl = sf + le * NFT + r;
-      eo_line<P, NQ2, PARTS>(sFz + off, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], part,
-                             [&](int m, CT v) {
+      auto emitz = [&](int m, CT v) {
         const int n = off + m * NQ2;
         const long long g = g0 + n;
         double inc;
@@ -293,7 +350,15 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
           qout[g] = inc;
         else
           qout[g] = rk_combine<RK>(inc, qin[g], RK == kRkGeneral ? q0[g] : 0.0, rk_a, rk_b);
-      });
+      };
+      if constexpr (kF64) {
+        double row[NQ];
+        eo_pairs_f64<P>(qin, gw, g0 + off, NQ2, row);
+        eo_line<P, 1, PARTS, true>(row, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], part, emitz);
+      } else {
+        eo_line<P, NQ2, PARTS, false>(sFz + off, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], part,
+                                      emitz);
+      }
     }
   });
 }
@@ -303,7 +368,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
 // memory latency.  FP64 (256 threads, 85 registers): a block in its load or
 // flux phase leaves two others feeding the FP64 pipe.
 template <int P, typename CT>
-__global__ void __launch_bounds__(EoCfg<P, CT>::THREADS, 3)
+__global__ void __launch_bounds__(EoCfg<P, CT>::THREADS, sizeof(CT) == 8 ? 4 : 3)
     stage_eo_kernel(const StageArgs a) {
   constexpr int EPB = EoCfg<P, CT>::EPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
