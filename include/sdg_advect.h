@@ -368,9 +368,9 @@ int sdg_ensemble_init_blob(sdg_ensemble* e, int i, const double* centre,
  * size by timing stage launches on this ensemble; leaves the state as is. */
 int sdg_ensemble_tune(sdg_ensemble* e);
 int sdg_ensemble_set_epb(sdg_ensemble* e, int p, int epb);
-/* Stage body of the batched kernel: SDG_OPT_GENERAL / SDG_OPT_OPT1 (the
- * default) the node body with running sums; SDG_OPT_EVENODD the even-odd body
- * for every order whose operators have the centro-symmetry. */
+/* Stage body of the batched kernels: SDG_OPT_EVENODD (the default) the
+ * even-odd body for every order whose operators have the centro-symmetry;
+ * SDG_OPT_GENERAL / SDG_OPT_OPT1 the node body with running sums. */
 int sdg_ensemble_set_opt(sdg_ensemble* e, int opt);
 int sdg_ensemble_set_threads(sdg_ensemble* e, int threads);
 /* epb_by_order receives 12 entries (index = order). */
@@ -402,9 +402,9 @@ typedef struct {
   int max_window_steps;     /* steps between admission points (default 8) */
   int threads;              /* block size of the batched kernel (0: 256) */
   int epb_by_order[16];     /* elements per block by order (0: default) */
-  int opt;                  /* stage body: 0, SDG_OPT_GENERAL or SDG_OPT_OPT1 =
-                               node body (running sums); SDG_OPT_EVENODD =
-                               even-odd where the operators allow it */
+  int opt;                  /* stage body: 0 or SDG_OPT_EVENODD = even-odd where
+                               the operators allow it, SDG_OPT_GENERAL /
+                               SDG_OPT_OPT1 = node body (running sums) */
 } sdg_server_config;
 typedef struct {
   int NeX, NeY, NeZ, p, nstep;

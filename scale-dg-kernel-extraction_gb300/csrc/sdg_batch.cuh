@@ -1,17 +1,20 @@
 // Batched advance of many independent boxes (an ensemble, or the requests a
-// server holds) in ONE persistent launch per RK stage.
+// server holds) with one persistent launch per order present and RK stage.
 //
 // Every box is an instance with its own order p, size, dt, rotating state
 // buffers and velocity.  A work item is one block's worth of consecutive
-// elements of one instance.  The persistent kernel's blocks take items
-// round-robin from the list (sorted by order), prefetch the next item's
-// instance header into shared memory while computing the current one, resolve
-// the instance's buffers for the stage, and run the same fused stage body as
-// the single-box solver (stage_block or stage_eo_block, FP32 compute, FP64
-// state), dispatched on the instance's order.  Each instance's current
+// elements of one instance.  The item list is sorted by order; each order's
+// items run in one persistent launch of a kernel compiled for that order,
+// whose blocks take items round-robin, prefetch the next item's instance
+// header into shared memory while computing the current one, resolve the
+// instance's buffers for the stage, and run the same fused stage body as the
+// single-box solver (stage_block or stage_eo_block, FP32 compute, FP64
+// state).  Each instance's current
 // buffer index lives on the device and is advanced by a tiny kernel after
 // stage 3, so one captured CUDA graph replays every step.
 #pragma once
+
+#include <vector>
 
 #include "sdg_stage_eo.cuh"
 
@@ -58,25 +61,29 @@ inline void batch_stage_factors(BatchInst& I) {
   }
 }
 
-// Launches one stage over `n_items` items.
-// mode: 0 all instances run the node body, 1 all the even-odd body, 2 mixed
-// (batch_mode below).
-int batch_stage_launch(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,
-                       int grid, int threads, size_t smem, int mode, cudaStream_t st);
-template <typename It, typename Get>
-inline int batch_mode(It begin, It end, Get eo_of) {
-  bool any_eo = false, any_node = false;
-  for (It i = begin; i != end; ++i) (eo_of(*i) ? any_eo : any_node) = true;
-  return any_eo ? (any_node ? 2 : 1) : 0;
-}
+// The items of one order and stage body, run by one persistent launch of a
+// kernel compiled for that order and body.  The item list is sorted by order
+// (and body), so a group is a contiguous range of it.
+struct BatchGroup {
+  int p = 0, eo = 0;       // order, 1 for the even-odd body
+  int begin = 0, count = 0;  // item range
+  size_t smem = 0;         // dynamic shared memory of a block
+  int grid = 0;            // persistent blocks (resident blocks, at most count)
+};
+
+// Sets the group kernel's shared-memory limit and its grid from occupancy.
+int batch_group_setup(BatchGroup& g, int threads);
+// Launches stage `stage` (0..2) of one group.
+int batch_group_launch(const BatchInst* d_inst, const BatchItem* d_items, const BatchGroup& g,
+                       int stage, int threads, cudaStream_t st);
+// Splits a sorted item list into groups (epb by order) and sets each up.
+int batch_groups(const std::vector<BatchItem>& items, const std::vector<BatchInst>& inst,
+                 const int* epb, int threads, std::vector<BatchGroup>& groups);
 // cur = (cur + 1) % 3 for every active instance.
 int batch_advance_launch(BatchInst* d_inst, int n_inst, cudaStream_t st);
 // Dynamic shared memory the kernel needs for `epb` elements of order p with
 // the node body (eo = 0) or the even-odd body (eo = 1).
 size_t batch_smem_bytes(int p, int epb, int eo);
-// Resident blocks of the batch kernel per SM for a block size and smem size.
-int batch_blocks_per_sm(int threads, size_t smem, int mode);
-int batch_set_max_smem(size_t smem, int mode);
 
 // Device-side initial condition: Gaussian tracer exp(-d^2/(2 sigma^2)) around
 // `centre` (periodic minimum image on the unit box) and a constant velocity,

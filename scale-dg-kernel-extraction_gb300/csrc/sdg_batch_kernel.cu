@@ -9,37 +9,25 @@ namespace {
 __constant__ double c_rk_a[3] = {0.0, 0.75, 1.0 / 3.0};
 __constant__ double c_rk_b[3] = {1.0, 0.25, 2.0 / 3.0};
 
-// MODE 0: every instance runs the node body; 1: every instance the even-odd
-// body; 2: either, per instance.  Separate instantiations keep each body's
-// register budget (the combined one needs the larger of the two).
-template <int P, int MODE, int RK>
-__device__ __forceinline__ void run_order(const StageArgs& a, const BatchItem& w, int eo,
-                                          unsigned char* smem) {
-  if (MODE == 1 || (MODE == 2 && eo))
-    stage_eo_block<P, float, RK>(a, w.e_begin, w.e_count, smem);
-  else
-    stage_block<P, float, float, false, RK>(a, w.e_begin, w.e_count, smem);
-}
-
 // 32-bit words of an instance header, copied into shared memory by as many
 // threads.
 constexpr int kInstWords = (int)(sizeof(BatchInst) / 4);
 static_assert(sizeof(BatchInst) % 4 == 0, "instance header is copied as 32-bit words");
 static_assert(kInstWords < 128, "the smallest block must copy the header in one pass");
 
-// Items are assigned round-robin (block b runs items b, b + G, b + 2G, ...;
-// the list is sorted by order, so every block gets a similar mix).  The next
-// item's instance header is fetched into shared memory while the current item
-// computes, and the item after that into a register, so that a block never
-// waits on the item -> instance -> data chain of dependent loads.
-// Register caps: the node body fits in 42 (three blocks of 512 threads an
-// SM); the even-odd modes are capped at 64 (two blocks), since the switch over
-// eleven orders otherwise makes the compiler keep the union of their needs.
-// RK: the stage's update kind (kRkFirst for stage 1, kRkGeneral otherwise),
-// a template parameter so that each instantiation carries one variant.
-template <int MODE, int RK>
-__global__ void __launch_bounds__(kBatchThreadsMax, MODE == 0 ? 3 : 2)
-    batch_stage_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
+// One persistent launch runs the items of one order group (order P, stage
+// body EO: 1 even-odd, 0 node body; RK the stage's update kind).  Compiling
+// one order and one body per kernel keeps each at its own register count
+// (40 for 3 blocks of 512 threads an SM), where a switch over the orders
+// would keep the union of their needs.
+//
+// Items are assigned round-robin (block b runs items b, b + G, b + 2G, ...).
+// The next item's instance header is fetched into shared memory while the
+// current item computes, and the item after that into a register, so that a
+// block never waits on the item -> instance -> data chain of dependent loads.
+template <int P, int EO, int RK>
+__global__ void __launch_bounds__(kBatchThreadsMax, 3)
+    batch_order_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
                        int n_items, int stage) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(16) BatchInst s_inst[2];
@@ -80,7 +68,7 @@ __global__ void __launch_bounds__(kBatchThreadsMax, MODE == 0 ? 3 : 2)
       a.u = I.u;
       a.v = I.v;
       a.w = I.w;
-      a.D = I.D;
+      a.D = EO ? static_cast<const void*>(I.eo_tab) : static_cast<const void*>(I.D);
       a.Lift = I.Lift;
       a.box = I.box;
       a.elem_begin = 0;
@@ -93,27 +81,14 @@ __global__ void __launch_bounds__(kBatchThreadsMax, MODE == 0 ? 3 : 2)
       a.b_is_one = (stage == 0);
       a.a_nonzero = (stage != 0);
       a.tend_only = 0;
-      const int eo = (MODE == 1) ? 1 : (MODE == 0) ? 0 : I.eo;
-      if (eo) {
-        a.D = I.eo_tab;
+      if constexpr (EO != 0) {
         for (int d = 0; d < 3; d++) {
           a.eo_sDf[d] = I.eo_sD[stage][d];
           a.eo_sLf[d] = I.eo_sL[stage][d];
         }
-      }
-      switch (I.p) {
-        case 1: run_order<1, MODE, RK>(a, w, eo, smem); break;
-        case 2: run_order<2, MODE, RK>(a, w, eo, smem); break;
-        case 3: run_order<3, MODE, RK>(a, w, eo, smem); break;
-        case 4: run_order<4, MODE, RK>(a, w, eo, smem); break;
-        case 5: run_order<5, MODE, RK>(a, w, eo, smem); break;
-        case 6: run_order<6, MODE, RK>(a, w, eo, smem); break;
-        case 7: run_order<7, MODE, RK>(a, w, eo, smem); break;
-        case 8: run_order<8, MODE, RK>(a, w, eo, smem); break;
-        case 9: run_order<9, MODE, RK>(a, w, eo, smem); break;
-        case 10: run_order<10, MODE, RK>(a, w, eo, smem); break;
-        case 11: run_order<11, MODE, RK>(a, w, eo, smem); break;
-        default: break;
+        stage_eo_block<P, float, RK>(a, w.e_begin, w.e_count, smem);
+      } else {
+        stage_block<P, float, float, false, RK>(a, w.e_begin, w.e_count, smem);
       }
     }
     // every read of this item's slots happened before the body's barriers
@@ -183,67 +158,101 @@ size_t batch_smem_bytes(int p, int epb, int eo) {
 }
 
 namespace {
-template <int MODE, int RK>
-int set_max_smem_one(size_t smem) {
-  SDG_CUDA_TRY(cudaFuncSetAttribute(batch_stage_kernel<MODE, RK>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  return SDG_OK;
-}
+// The three functions an order group needs, for one (P, EO) pair.
+template <int P, int EO>
+struct GroupOps {
+  static int set_smem(size_t smem) {
+    SDG_CUDA_TRY(cudaFuncSetAttribute(batch_order_kernel<P, EO, kRkFirst>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SDG_CUDA_TRY(cudaFuncSetAttribute(batch_order_kernel<P, EO, kRkGeneral>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return SDG_OK;
+  }
+  static int blocks_per_sm(int threads, size_t smem) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_order_kernel<P, EO, kRkGeneral>,
+                                                      threads, smem) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    return nb;
+  }
+  static int launch(const BatchInst* d_inst, const BatchItem* d_items, int n, int stage,
+                    int grid, int threads, size_t smem, cudaStream_t st) {
+    if (stage == 0)
+      batch_order_kernel<P, EO, kRkFirst><<<grid, threads, smem, st>>>(d_inst, d_items, n, stage);
+    else
+      batch_order_kernel<P, EO, kRkGeneral><<<grid, threads, smem, st>>>(d_inst, d_items, n,
+                                                                         stage);
+    SDG_CUDA_TRY(cudaGetLastError());
+    return SDG_OK;
+  }
+};
 
-template <int MODE>
-int set_max_smem_mode(size_t smem) {
-  const int st = set_max_smem_one<MODE, kRkFirst>(smem);
-  if (st != SDG_OK) return st;
-  return set_max_smem_one<MODE, kRkGeneral>(smem);
-}
-
-template <int MODE>
-int launch_mode(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,
-                int grid, int threads, size_t smem, cudaStream_t st) {
-  if (stage == 0)
-    batch_stage_kernel<MODE, kRkFirst><<<grid, threads, smem, st>>>(d_inst, d_items, n_items,
-                                                                    stage);
-  else
-    batch_stage_kernel<MODE, kRkGeneral><<<grid, threads, smem, st>>>(d_inst, d_items, n_items,
-                                                                      stage);
-  SDG_CUDA_TRY(cudaGetLastError());
-  return SDG_OK;
+template <template <int, int> class OPS, typename F>
+int with_group(int p, int eo, F&& f) {
+  switch (p * 2 + (eo ? 1 : 0)) {
+#define SDG_GROUP_CASE(P) \
+  case 2 * P: return f(OPS<P, 0>{}); \
+  case 2 * P + 1: return f(OPS<P, 1>{});
+    SDG_GROUP_CASE(1) SDG_GROUP_CASE(2) SDG_GROUP_CASE(3) SDG_GROUP_CASE(4)
+    SDG_GROUP_CASE(5) SDG_GROUP_CASE(6) SDG_GROUP_CASE(7) SDG_GROUP_CASE(8)
+    SDG_GROUP_CASE(9) SDG_GROUP_CASE(10) SDG_GROUP_CASE(11)
+#undef SDG_GROUP_CASE
+    default: return fail(SDG_ERR_UNSUPPORTED_ORDER, "batched order %d outside 1..11", p);
+  }
 }
 }  // namespace
 
-int batch_set_max_smem(size_t smem, int mode) {
-  if (mode == 1) return set_max_smem_mode<1>(smem);
-  if (mode == 2) return set_max_smem_mode<2>(smem);
-  return set_max_smem_mode<0>(smem);
+int batch_group_setup(BatchGroup& g, int threads) {
+  int dev = 0, nsm = 0;
+  SDG_CUDA_TRY(cudaGetDevice(&dev));
+  SDG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  int per_sm = 0;
+  const int st = with_group<GroupOps>(g.p, g.eo, [&](auto ops) {
+    const int r = decltype(ops)::set_smem(g.smem);
+    if (r != SDG_OK) return r;
+    per_sm = decltype(ops)::blocks_per_sm(threads, g.smem);
+    return SDG_OK;
+  });
+  if (st != SDG_OK) return st;
+  if (per_sm <= 0)
+    return fail(SDG_ERR_INVALID_ARG, "batch kernel of order %d does not fit: %d threads, %zu B",
+                g.p, threads, g.smem);
+  const long long cap = (long long)nsm * per_sm;
+  g.grid = (int)(g.count < cap ? g.count : cap);
+  return SDG_OK;
 }
 
-// Occupancy of the general-stage instantiation (the first-stage one has the
-// same shape and no more registers).
-int batch_blocks_per_sm(int threads, size_t smem, int mode) {
-  int nb = 0;
-  if (batch_set_max_smem(smem, mode) != SDG_OK) return 0;
-  cudaError_t ce =
-      (mode == 1)
-          ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<1, kRkGeneral>,
-                                                          threads, smem)
-      : (mode == 2)
-          ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<2, kRkGeneral>,
-                                                          threads, smem)
-          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_stage_kernel<0, kRkGeneral>,
-                                                          threads, smem);
-  if (ce != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
+int batch_group_launch(const BatchInst* d_inst, const BatchItem* d_items, const BatchGroup& g,
+                       int stage, int threads, cudaStream_t st) {
+  if (g.count <= 0) return SDG_OK;
+  return with_group<GroupOps>(g.p, g.eo, [&](auto ops) {
+    return decltype(ops)::launch(d_inst, d_items + g.begin, g.count, stage, g.grid, threads,
+                                 g.smem, st);
+  });
+}
+
+int batch_groups(const std::vector<BatchItem>& items, const std::vector<BatchInst>& inst,
+                 const int* epb, int threads, std::vector<BatchGroup>& groups) {
+  groups.clear();
+  for (size_t i = 0; i < items.size();) {
+    const BatchInst& I = inst[items[i].inst];
+    BatchGroup g;
+    g.p = I.p;
+    g.eo = I.eo;
+    g.begin = (int)i;
+    size_t j = i;
+    while (j < items.size() && inst[items[j].inst].p == g.p && inst[items[j].inst].eo == g.eo)
+      j++;
+    g.count = (int)(j - i);
+    g.smem = batch_smem_bytes(g.p, epb[g.p], g.eo);
+    g.grid = 0;
+    SDG_TRY(batch_group_setup(g, threads));
+    groups.push_back(g);
+    i = j;
   }
-  return nb;
-}
-
-int batch_stage_launch(const BatchInst* d_inst, const BatchItem* d_items, int n_items, int stage,
-                       int grid, int threads, size_t smem, int mode, cudaStream_t st) {
-  if (n_items <= 0) return SDG_OK;
-  if (mode == 1) return launch_mode<1>(d_inst, d_items, n_items, stage, grid, threads, smem, st);
-  if (mode == 2) return launch_mode<2>(d_inst, d_items, n_items, stage, grid, threads, smem, st);
-  return launch_mode<0>(d_inst, d_items, n_items, stage, grid, threads, smem, st);
+  return SDG_OK;
 }
 
 int batch_advance_launch(BatchInst* d_inst, int n_inst, cudaStream_t st) {

@@ -22,13 +22,11 @@ struct sdg_ensemble {
   int n_items = 0;
   void* arena = nullptr;
   float* d_ops[kBatchMaxOrder + 1][3] = {};  // D1D, Lift, even-odd tables (FP32)
-  bool use_eo = false;             // even-odd body (where the operators allow it)
+  bool use_eo = true;              // even-odd body (where the operators allow it)
   double* d_x1D[kBatchMaxOrder + 1] = {};
   int epb[kBatchMaxOrder + 1] = {};
   int threads = 256;
-  size_t smem = 0;
-  int grid = 0;
-  int mode = 0;                    // batch kernel body mode (batch_mode)
+  std::vector<BatchGroup> groups;  // one persistent launch per order present
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   long long total_dof = 0;
@@ -66,13 +64,11 @@ int build_items(sdg_ensemble* e, const std::vector<int>* subset = nullptr) {
     for (int i = 0; i < e->n; i++) idx.push_back(i);
   std::stable_sort(idx.begin(), idx.end(),
                    [&](int a, int b) { return e->inst[a].p > e->inst[b].p; });
-  size_t smem = 0;
   for (int i : idx) {
     const BatchInst& I = e->inst[i];
     const int epb = e->epb[I.p];
     for (long long b = 0; b < I.box.Ne; b += epb)
       items.push_back({i, (int)b, (int)std::min<long long>(epb, I.box.Ne - b)});
-    smem = std::max(smem, batch_smem_bytes(I.p, epb, I.eo));
   }
   cudaFree(e->d_items);
   e->d_items = nullptr;
@@ -82,23 +78,13 @@ int build_items(sdg_ensemble* e, const std::vector<int>* subset = nullptr) {
     SDG_CUDA_TRY(cudaMemcpy(e->d_items, items.data(), sizeof(BatchItem) * items.size(),
                             cudaMemcpyHostToDevice));
   }
-  e->smem = smem;
-  e->mode = batch_mode(idx.begin(), idx.end(), [&](int i) { return e->inst[i].eo != 0; });
-  int dev = 0, nsm = 0;
-  SDG_CUDA_TRY(cudaGetDevice(&dev));
-  SDG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const int per_sm = batch_blocks_per_sm(e->threads, smem, e->mode);
-  if (per_sm <= 0)
-    return fail(SDG_ERR_INVALID_ARG, "batch kernel does not fit: %d threads, %zu B smem",
-                e->threads, smem);
-  e->grid = nsm * per_sm;
-  return SDG_OK;
+  return batch_groups(items, e->inst, e->epb, e->threads, e->groups);
 }
 
 int enqueue_step(sdg_ensemble* e) {
   for (int s = 0; s < 3; s++)
-    SDG_TRY(batch_stage_launch(e->d_inst, e->d_items, e->n_items, s, e->grid, e->threads,
-                               e->smem, e->mode, e->stream));
+    for (const BatchGroup& g : e->groups)
+      SDG_TRY(batch_group_launch(e->d_inst, e->d_items, g, s, e->threads, e->stream));
   return batch_advance_launch(e->d_inst, e->n, e->stream);
 }
 
@@ -138,8 +124,8 @@ int time_stage0(sdg_ensemble* e, float* ms) {
   for (int r = 0; r < 3; r++) {
     // stage 0 reads q[cur] and writes q[cur+1]: repeating it leaves the state
     SDG_CUDA_TRY(cudaEventRecord(a, e->stream));
-    SDG_TRY(batch_stage_launch(e->d_inst, e->d_items, e->n_items, 0, e->grid, e->threads,
-                               e->smem, e->mode, e->stream));
+    for (const BatchGroup& g : e->groups)
+      SDG_TRY(batch_group_launch(e->d_inst, e->d_items, g, 0, e->threads, e->stream));
     SDG_CUDA_TRY(cudaEventRecord(b, e->stream));
     SDG_CUDA_TRY(cudaEventSynchronize(b));
     float t = 0.f;
@@ -333,7 +319,10 @@ int sdg_ensemble_get_config(const sdg_ensemble* e, int* epb_by_order, int* threa
   if (epb_by_order)
     for (int p = 0; p <= kBatchMaxOrder; p++) epb_by_order[p] = e->epb[p];
   if (threads) *threads = e->threads;
-  if (grid) *grid = e->grid;
+  if (grid) {
+    *grid = 0;
+    for (const BatchGroup& g : e->groups) *grid = std::max(*grid, g.grid);
+  }
   return SDG_OK;
 }
 
@@ -433,7 +422,9 @@ int sdg_ensemble_download(sdg_ensemble* e, int i, double* q) {
 
 long long sdg_ensemble_total_dofs(const sdg_ensemble* e) { return e ? e->total_dof : 0; }
 
-int sdg_ensemble_launches_per_step(const sdg_ensemble* e) { return e ? 4 : 0; }
+int sdg_ensemble_launches_per_step(const sdg_ensemble* e) {
+  return e ? 3 * (int)e->groups.size() + 1 : 0;
+}
 
 int sdg_ensemble_destroy(sdg_ensemble* e) {
   if (!e) return SDG_OK;

@@ -68,9 +68,7 @@ struct sdg_server {
   BatchItem* d_items = nullptr;
   int d_items_cap = 0;
   int n_items = 0;
-  size_t smem = 0;
-  int grid = 0;
-  int mode = 0;  // batch kernel body mode of the active set (batch_mode)
+  std::vector<BatchGroup> groups;  // one persistent launch per order active
   int threads = 256;
   int epb[kBatchMaxOrder + 1] = {};
   // statistics
@@ -133,7 +131,6 @@ int rebuild_tables(sdg_server* s) {
   for (int i = 0; i < n; i++) order[i] = i;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return s->active[a]->r.p > s->active[b]->r.p; });
-  size_t smem = 0;
   for (int i = 0; i < n; i++) {
     inst[i] = s->active[i]->inst;
     inst[i].cur = s->active[i]->steps_done % 3;
@@ -143,7 +140,6 @@ int rebuild_tables(sdg_server* s) {
     const int e = s->epb[I.p];
     for (long long b = 0; b < I.box.Ne; b += e)
       items.push_back({i, (int)b, (int)std::min<long long>(e, I.box.Ne - b)});
-    smem = std::max(smem, batch_smem_bytes(I.p, e, I.eo));
   }
   if (n > s->d_inst_cap) {
     cudaFree(s->d_inst);
@@ -166,28 +162,17 @@ int rebuild_tables(sdg_server* s) {
   // the host vectors must outlive the asynchronous copies
   SDG_CUDA_TRY(cudaStreamSynchronize(s->stream));
   s->n_items = (int)items.size();
-  const int mode = batch_mode(inst.begin(), inst.end(), [](const BatchInst& I) { return I.eo != 0; });
-  if (smem > s->smem || s->grid == 0 || mode != s->mode) {
-    s->smem = std::max(smem, s->smem);
-    s->mode = mode;
-    int dev = 0, nsm = 0;
-    SDG_CUDA_TRY(cudaGetDevice(&dev));
-    SDG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const int per_sm = batch_blocks_per_sm(s->threads, s->smem, s->mode);
-    if (per_sm <= 0) return fail(SDG_ERR_INVALID_ARG, "batch kernel does not fit");
-    s->grid = nsm * per_sm;
-  }
-  return SDG_OK;
+  return batch_groups(items, inst, s->epb, s->threads, s->groups);
 }
 
 int run_steps(sdg_server* s, int nsteps) {
   const int n = (int)s->active.size();
   for (int k = 0; k < nsteps; k++) {
     for (int st = 0; st < 3; st++)
-      SDG_TRY(batch_stage_launch(s->d_inst, s->d_items, s->n_items, st, s->grid, s->threads,
-                                 s->smem, s->mode, s->stream));
+      for (const BatchGroup& g : s->groups)
+        SDG_TRY(batch_group_launch(s->d_inst, s->d_items, g, st, s->threads, s->stream));
     SDG_TRY(batch_advance_launch(s->d_inst, n, s->stream));
-    s->launches += 4;
+    s->launches += 3 * (long long)s->groups.size() + 1;
   }
   return SDG_OK;
 }
@@ -376,9 +361,9 @@ int sdg_server_create(sdg_server** out, const sdg_server_config* cfg,
     if (ce == cudaSuccess) ce = cudaMemcpy(s->d_ops[p][1], l.data(), 4 * nl, cudaMemcpyHostToDevice);
     if (ce == cudaSuccess)
       ce = cudaMemcpy(s->d_x1D[p], x1D_by_order[p], 8 * nq, cudaMemcpyHostToDevice);
-    // even-odd tables (opt EVENODD) when the operators have the symmetry
+    // even-odd tables (opt 0 or EVENODD) when the operators have the symmetry
     std::vector<double> eo;
-    const bool want_eo = (cfg->opt == SDG_OPT_EVENODD);
+    const bool want_eo = (cfg->opt == 0 || cfg->opt == SDG_OPT_EVENODD);
     if (ce == cudaSuccess && want_eo &&
         eo_tables(nq, D1D_by_order[p], Lift_by_order[p], eo) == SDG_OK) {
       std::vector<float> ef(eo.begin(), eo.end());

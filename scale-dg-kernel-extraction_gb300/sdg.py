@@ -469,8 +469,9 @@ class Solver:
 
 
 class Ensemble:
-    """Independent boxes advanced together, one persistent launch per RK stage
-    (sdg_ensemble_* in include/sdg_advect.h); FP32 compute, FP64 state."""
+    """Independent boxes advanced together, one persistent launch per order and
+    RK stage (sdg_ensemble_* in include/sdg_advect.h); FP32 compute, FP64
+    state."""
 
     def __init__(self, dims, orders, dt, ops_by_order, stream=None):
         """dims: list of (NeX,NeY,NeZ); orders: list of p; dt: list;
@@ -521,8 +522,11 @@ class Ensemble:
     def set_threads(self, threads) -> None:
         _check(lib.sdg_ensemble_set_threads(self._h, threads), "sdg_ensemble_set_threads")
 
+    def launches_per_step(self) -> int:
+        return lib.sdg_ensemble_launches_per_step(self._h)
+
     def set_opt(self, opt) -> None:
-        """OPT_GENERAL/OPT_OPT1 (default): node body; OPT_EVENODD: even-odd body."""
+        """OPT_EVENODD (default): even-odd body; OPT_GENERAL/OPT_OPT1: node body."""
         _check(lib.sdg_ensemble_set_opt(self._h, opt), "sdg_ensemble_set_opt")
 
     def config(self) -> dict:

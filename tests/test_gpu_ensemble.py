@@ -29,7 +29,7 @@ def build(members, seed0=100):
     return ens, fields, dts, ops
 
 
-def standalone(dims, p, fields, dt, ops, nstep, opt=sdg.OPT_GENERAL):
+def standalone(dims, p, fields, dt, ops, nstep, opt=sdg.OPT_EVENODD):
     s = sdg.Solver(*dims, p, ops[p][1], ops[p][3], opt=opt, precision=sdg.PREC_FP32)
     s.upload(*fields)
     s.step(dt, nstep)
@@ -38,9 +38,9 @@ def standalone(dims, p, fields, dt, ops, nstep, opt=sdg.OPT_GENERAL):
 
 @pytest.mark.parametrize("opt", [sdg.OPT_EVENODD, sdg.OPT_GENERAL])
 def test_members_equal_the_standalone_fp32_solver_bitwise(opt):
-    """Node body (the default, GENERAL running sums) and even-odd body."""
+    """Even-odd body (the default) and node body (GENERAL running sums)."""
     ens, fields, dts, ops = build(MEMBERS)
-    if opt == sdg.OPT_EVENODD:
+    if opt != sdg.OPT_EVENODD:
         ens.set_opt(opt)
     ens.step(4)
     for i, (dims, p) in enumerate(MEMBERS):
@@ -50,7 +50,6 @@ def test_members_equal_the_standalone_fp32_solver_bitwise(opt):
 
 def test_switching_the_body_mid_run_keeps_the_state():
     ens, fields, dts, ops = build(MEMBERS[:3], seed0=150)
-    ens.set_opt(sdg.OPT_EVENODD)
     ens.step(2)
     ens.set_opt(sdg.OPT_GENERAL)
     ens.step(1)

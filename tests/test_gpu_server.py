@@ -43,11 +43,11 @@ def mixed_ops(ops):
 def test_result_is_the_same_alone_and_in_the_mix(ops, body):
     target = req((3, 4, 2), 5, 40, 11)
     if body == "node":
-        srv = sdg.Server(ops)
+        srv = sdg.Server(ops, opt=sdg.OPT_GENERAL)
     elif body == "mixed":
-        srv = sdg.Server(mixed_ops(ops), opt=sdg.OPT_EVENODD)
+        srv = sdg.Server(mixed_ops(ops))
     else:
-        srv = sdg.Server(ops, opt=sdg.OPT_EVENODD)
+        srv = sdg.Server(ops)
     alone, _ = None, None
     t = srv.submit(**target, want_state=True)
     res, alone = srv.wait(t)
@@ -70,7 +70,7 @@ def test_result_is_the_same_alone_and_in_the_mix(ops, body):
     srv.close()
 
 
-@pytest.mark.parametrize("opt", [0, sdg.OPT_EVENODD])
+@pytest.mark.parametrize("opt", [0, sdg.OPT_GENERAL])
 def test_served_result_matches_fp64_oracle_within_fp32_tolerance(ops, opt):
     r = req((3, 2, 3), 3, 20, 31)
     srv = sdg.Server(ops, opt=opt)
