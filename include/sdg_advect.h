@@ -344,9 +344,9 @@ int sdg_solver_destroy(sdg_solver* s);
 
 /* Many independent periodic boxes (orders 1..11, any sizes, each with its own
  * dt) advanced together in FP32-compute / FP64-state form.  A step is a CUDA
- * graph of four kernels: three persistent stage launches that each cover
- * every instance (blocks pull (instance, element block) work items from a
- * counter and dispatch on the instance's order) and an index advance.
+ * graph of one persistent launch per RK stage and (order, stage body) group
+ * (the blocks of a group take its (instance, element block) work items
+ * round-robin) and an index advance: 3 x groups + 1 kernels.
  * dims holds NeX,NeY,NeZ per instance; D1D_by_order / Lift_by_order /
  * x1D_by_order are indexed by the order (entries for absent orders may be
  * NULL; x1D_by_order may be NULL when sdg_ensemble_init_blob is not used).
@@ -364,15 +364,20 @@ int sdg_ensemble_upload(sdg_ensemble* e, int i, const double* q,
  * sigma around centre[3] (periodic unit box) in the constant velocity[3]. */
 int sdg_ensemble_init_blob(sdg_ensemble* e, int i, const double* centre,
                            double sigma, const double* velocity);
-/* Autotuner: picks elements per block for every order present and the block
- * size by timing stage launches on this ensemble; leaves the state as is. */
+/* Autotuner: picks the stage body (unless sdg_ensemble_set_opt fixed it) and
+ * the elements per block for every order present and the block size by
+ * timing stage launches on this ensemble; leaves the state as is. */
 int sdg_ensemble_tune(sdg_ensemble* e);
 int sdg_ensemble_set_epb(sdg_ensemble* e, int p, int epb);
 /* Stage body of the batched kernels: SDG_OPT_EVENODD (the default) the
  * even-odd body for every order whose operators have the centro-symmetry;
- * SDG_OPT_GENERAL / SDG_OPT_OPT1 the node body with running sums. */
+ * SDG_OPT_GENERAL / SDG_OPT_OPT1 the node body with running sums.  The
+ * choice holds for every order and the autotuner keeps it afterwards. */
 int sdg_ensemble_set_opt(sdg_ensemble* e, int opt);
 int sdg_ensemble_set_threads(sdg_ensemble* e, int threads);
+/* eo_by_order receives 12 entries (index = order): 1 where the order's
+ * instances run the even-odd body, 0 for the node body or an absent order. */
+int sdg_ensemble_get_bodies(const sdg_ensemble* e, int* eo_by_order);
 /* epb_by_order receives 12 entries (index = order). */
 int sdg_ensemble_get_config(const sdg_ensemble* e, int* epb_by_order,
                             int* threads, int* grid);

@@ -22,7 +22,8 @@ struct sdg_ensemble {
   int n_items = 0;
   void* arena = nullptr;
   float* d_ops[kBatchMaxOrder + 1][3] = {};  // D1D, Lift, even-odd tables (FP32)
-  bool use_eo = true;              // even-odd body (where the operators allow it)
+  int eo_by_order[kBatchMaxOrder + 1] = {};  // stage body per order (1: even-odd)
+  bool body_fixed = false;         // set_opt chose the body; the tuner keeps it
   double* d_x1D[kBatchMaxOrder + 1] = {};
   int epb[kBatchMaxOrder + 1] = {};
   int threads = 256;
@@ -225,7 +226,8 @@ int sdg_ensemble_create(sdg_ensemble** out, int n, const int* dims, const int* o
     I.D = e->d_ops[p][0];
     I.Lift = e->d_ops[p][1];
     I.eo_tab = e->d_ops[p][2];
-    I.eo = (I.eo_tab != nullptr && e->use_eo) ? 1 : 0;
+    e->eo_by_order[p] = (I.eo_tab != nullptr) ? 1 : 0;  // even-odd by default
+    I.eo = e->eo_by_order[p];
     I.dt = dt[i];
     batch_stage_factors(I);
     I.p = p;
@@ -291,27 +293,37 @@ int sdg_ensemble_set_threads(sdg_ensemble* e, int threads) {
   return build_items(e);
 }
 
+// The kernels take the stage body from their group, so a body change only
+// regroups the items (the device instance table keeps its buffer indices).
+static void set_bodies(sdg_ensemble* e) {
+  for (int i = 0; i < e->n; i++) {
+    BatchInst& I = e->inst[i];
+    I.eo = (I.eo_tab != nullptr && e->eo_by_order[I.p]) ? 1 : 0;
+  }
+}
+
 int sdg_ensemble_set_opt(sdg_ensemble* e, int opt) {
   if (!e) return fail(SDG_ERR_INVALID_ARG, "NULL ensemble");
   if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1 && opt != SDG_OPT_EVENODD)
     return fail(SDG_ERR_BAD_OPTTYPE, "unknown opt type %d", opt);
-  e->use_eo = (opt == SDG_OPT_EVENODD);
-  // the device copy holds the live buffer indices: update only the body flag
-  SDG_CUDA_TRY(cudaStreamSynchronize(e->stream));
-  std::vector<BatchInst> live(e->n);
-  SDG_CUDA_TRY(cudaMemcpy(live.data(), e->d_inst, sizeof(BatchInst) * e->n,
-                          cudaMemcpyDeviceToHost));
-  for (int i = 0; i < e->n; i++) {
-    e->inst[i].eo = (e->inst[i].eo_tab != nullptr && e->use_eo) ? 1 : 0;
-    live[i].eo = e->inst[i].eo;
-  }
-  SDG_CUDA_TRY(cudaMemcpy(e->d_inst, live.data(), sizeof(BatchInst) * e->n,
-                          cudaMemcpyHostToDevice));
+  for (int p = 0; p <= kBatchMaxOrder; p++) e->eo_by_order[p] = (opt == SDG_OPT_EVENODD);
+  e->body_fixed = true;
+  set_bodies(e);
   if (e->graph) {
     cudaGraphExecDestroy(e->graph);
     e->graph = nullptr;
   }
   return build_items(e);
+}
+
+int sdg_ensemble_get_bodies(const sdg_ensemble* e, int* eo_by_order) {
+  if (!e || !eo_by_order) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  for (int p = 0; p <= kBatchMaxOrder; p++) {
+    int any = 0;
+    for (int i = 0; i < e->n && !any; i++) any = (e->inst[i].p == p) ? e->inst[i].eo : 0;
+    eo_by_order[p] = any;
+  }
+  return SDG_OK;
 }
 
 int sdg_ensemble_get_config(const sdg_ensemble* e, int* epb_by_order, int* threads, int* grid) {
@@ -327,10 +339,12 @@ int sdg_ensemble_get_config(const sdg_ensemble* e, int* epb_by_order, int* threa
 }
 
 // Autotuner: for each order present, time stage 0 over that order's
-// instances for every elements-per-block candidate (about 64 to 4096 nodes a
-// block, shared memory under 96 KB) at each block size in {128, 256, 512};
-// keep per order the fastest candidate, then keep the block size whose summed
-// best times are smallest.  Stage 0 leaves the state unchanged, so tuning can
+// instances for both stage bodies (even-odd where the operators allow it, and
+// the node body) and every elements-per-block candidate (about 64 to 4096
+// nodes a block, shared memory under 96 KB) at each block size in
+// {128, 256, 512}; keep per order the fastest body and candidate, then keep
+// the block size whose summed best times are smallest.  After set_opt the
+// body stays the one it chose.  Stage 0 leaves the state unchanged, so tuning can
 // run at any point.
 int sdg_ensemble_tune(sdg_ensemble* e) {
   if (!e) return fail(SDG_ERR_INVALID_ARG, "NULL ensemble");
@@ -342,27 +356,41 @@ int sdg_ensemble_tune(sdg_ensemble* e) {
   int best_epb[kBatchMaxOrder + 1];
   for (int p = 0; p <= kBatchMaxOrder; p++) best_epb[p] = e->epb[p];
   const int saved_threads = e->threads;
-  int saved_epb[kBatchMaxOrder + 1];
-  for (int p = 0; p <= kBatchMaxOrder; p++) saved_epb[p] = e->epb[p];
+  int saved_epb[kBatchMaxOrder + 1], saved_eo[kBatchMaxOrder + 1], best_eo[kBatchMaxOrder + 1];
+  for (int p = 0; p <= kBatchMaxOrder; p++) {
+    saved_epb[p] = e->epb[p];
+    saved_eo[p] = best_eo[p] = e->eo_by_order[p];
+  }
   for (int th : thread_opts) {
     e->threads = th;
     double total = 0;
-    int epb_here[kBatchMaxOrder + 1];
-    for (int p = 0; p <= kBatchMaxOrder; p++) epb_here[p] = e->epb[p];
+    int epb_here[kBatchMaxOrder + 1], eo_here[kBatchMaxOrder + 1];
+    for (int p = 0; p <= kBatchMaxOrder; p++) {
+      epb_here[p] = e->epb[p];
+      eo_here[p] = saved_eo[p];
+    }
     for (int p = 1; p <= kBatchMaxOrder; p++) {
       if (by_order[p].empty()) continue;
       const int np = (p + 1) * (p + 1) * (p + 1);
       float best = 1e30f;
-      for (int cand = 1; cand <= 256; cand *= 2) {
-        if (cand * np > 4096 || (cand * np < 64 && cand * 2 * np <= 4096)) continue;
-        if (batch_smem_bytes(p, cand, e->inst[by_order[p][0]].eo) > 96 * 1024) continue;
-        e->epb[p] = cand;
-        if (build_items(e, &by_order[p]) != SDG_OK) continue;
-        float ms = 0.f;
-        SDG_TRY(time_stage0(e, &ms));
-        if (ms < best) {
-          best = ms;
-          epb_here[p] = cand;
+      const bool has_eo = e->inst[by_order[p][0]].eo_tab != nullptr;
+      const int body_hi = e->body_fixed ? saved_eo[p] : (has_eo ? 1 : 0);
+      const int body_lo = e->body_fixed ? saved_eo[p] : 0;
+      for (int body = body_hi; body >= body_lo; body--) {
+        e->eo_by_order[p] = body;
+        set_bodies(e);
+        for (int cand = 1; cand <= 256; cand *= 2) {
+          if (cand * np > 4096 || (cand * np < 64 && cand * 2 * np <= 4096)) continue;
+          if (batch_smem_bytes(p, cand, body) > 96 * 1024) continue;
+          e->epb[p] = cand;
+          if (build_items(e, &by_order[p]) != SDG_OK) continue;
+          float ms = 0.f;
+          SDG_TRY(time_stage0(e, &ms));
+          if (ms < best) {
+            best = ms;
+            epb_here[p] = cand;
+            eo_here[p] = body;
+          }
         }
       }
       e->epb[p] = epb_here[p];
@@ -371,13 +399,24 @@ int sdg_ensemble_tune(sdg_ensemble* e) {
     if (total < best_total) {
       best_total = total;
       best_threads = th;
-      for (int p = 0; p <= kBatchMaxOrder; p++) best_epb[p] = epb_here[p];
+      for (int p = 0; p <= kBatchMaxOrder; p++) {
+        best_epb[p] = epb_here[p];
+        best_eo[p] = eo_here[p];
+      }
     }
-    for (int p = 0; p <= kBatchMaxOrder; p++) e->epb[p] = saved_epb[p];
+    for (int p = 0; p <= kBatchMaxOrder; p++) {
+      e->epb[p] = saved_epb[p];
+      e->eo_by_order[p] = saved_eo[p];
+    }
+    set_bodies(e);
   }
   (void)saved_threads;
   e->threads = best_threads;
-  for (int p = 0; p <= kBatchMaxOrder; p++) e->epb[p] = best_epb[p];
+  for (int p = 0; p <= kBatchMaxOrder; p++) {
+    e->epb[p] = best_epb[p];
+    e->eo_by_order[p] = best_eo[p];
+  }
+  set_bodies(e);
   if (e->graph) {
     cudaGraphExecDestroy(e->graph);
     e->graph = nullptr;

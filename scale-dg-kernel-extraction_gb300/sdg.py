@@ -146,6 +146,7 @@ def _load() -> C.CDLL:
         "sdg_ensemble_set_opt": ([_vp, _i], _i),
         "sdg_ensemble_set_threads": ([_vp, _i], _i),
         "sdg_ensemble_get_config": ([_vp, _ip, C.POINTER(_i), C.POINTER(_i)], _i),
+        "sdg_ensemble_get_bodies": ([_vp, _ip], _i),
         "sdg_ensemble_step": ([_vp, _i], _i),
         "sdg_ensemble_step_timed": ([_vp, _i, C.POINTER(_d)], _i),
         "sdg_ensemble_download": ([_vp, _i, _dp], _i),
@@ -534,7 +535,11 @@ class Ensemble:
         th, gr = _i(), _i()
         _check(lib.sdg_ensemble_get_config(self._h, epb, C.byref(th), C.byref(gr)),
                "sdg_ensemble_get_config")
-        return {"epb": {p: int(epb[p]) for p in sorted(set(self.orders))},
+        eo = np.zeros(12, dtype=np.int32)
+        _check(lib.sdg_ensemble_get_bodies(self._h, eo), "sdg_ensemble_get_bodies")
+        orders = sorted(set(self.orders))
+        return {"epb": {p: int(epb[p]) for p in orders},
+                "body": {p: ("evenodd" if eo[p] else "node") for p in orders},
                 "threads": th.value, "grid": gr.value}
 
     def step(self, nstep: int) -> None:

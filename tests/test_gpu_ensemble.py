@@ -81,15 +81,32 @@ def test_members_within_fp32_tolerance_of_fp64_oracle():
 
 
 def test_autotuner_keeps_results_and_picks_valid_shapes():
+    """The tuner picks a stage body per order; each member then equals the
+    standalone solver running that body."""
     ens, fields, dts, ops = build(MEMBERS, seed0=300)
+    assert all(b == "evenodd" for b in ens.config()["body"].values())
     cfg = ens.tune()
     assert cfg["threads"] in (128, 256, 512) and cfg["grid"] > 0
+    assert set(cfg["body"]) == {p for _, p in MEMBERS}
     for p, e in cfg["epb"].items():
         assert e >= 1
     ens.step(3)
     for i, (dims, p) in enumerate(MEMBERS):
-        want = standalone(dims, p, fields[i], dts[i], ops, 3)
-        assert np.array_equal(ens.download(i), want)
+        opt = sdg.OPT_EVENODD if cfg["body"][p] == "evenodd" else sdg.OPT_GENERAL
+        want = standalone(dims, p, fields[i], dts[i], ops, 3, opt)
+        assert np.array_equal(ens.download(i), want), (i, p, cfg["body"][p])
+
+
+def test_set_opt_overrides_the_tuned_bodies_and_the_tuner_keeps_it():
+    ens, fields, dts, ops = build(MEMBERS[:4], seed0=350)
+    ens.tune()
+    ens.set_opt(sdg.OPT_GENERAL)
+    assert all(b == "node" for b in ens.config()["body"].values())
+    assert all(b == "node" for b in ens.tune()["body"].values())
+    ens.step(2)
+    for i, (dims, p) in enumerate(MEMBERS[:4]):
+        want = standalone(dims, p, fields[i], dts[i], ops, 2, sdg.OPT_GENERAL)
+        assert np.array_equal(ens.download(i), want), i
 
 
 def test_explicit_shapes_and_graph_replay_compose():
