@@ -486,10 +486,12 @@ def bench_dropin(sdg, args, wl, fused_rate):
             "achieved_gbs_with_geometry": bpd * rate}
 
 
-def bench_serving(sdg, args, rate=None):
+def bench_serving(sdg, args, rate=None, plain_cache=None):
     """Poisson arrivals of solves (Ne per axis U{4..32}, p U{2..11}, nstep
     U{10..500}, Gaussian tracer in a constant velocity, FP32 compute / FP64
-    state) into the continuous-batching server."""
+    state) into the continuous-batching server.  The request stream is the
+    same at every rate (only the arrival times scale), so plain_cache keeps
+    the plain-path time of its sample across calls."""
     import math
     import workloads as W
     ops = {p: sdg.operator_generate(p) for p in range(2, 12)}
@@ -526,7 +528,8 @@ def bench_serving(sdg, args, rate=None):
     # the plain FP64 path on the first requests, one after the other
     k = min(args.serve_plain_sample, len(reqs))
     pt = 0.0
-    for r in reqs[:k]:
+    cached = plain_cache.get("t") if plain_cache is not None else None
+    for r in (reqs[:k] if cached is None else []):
         x, D, Dt, L = ops[r["p"]]
         s = sdg.Solver(r["NeX"], r["NeY"], r["NeZ"], r["p"], D, L, opt=OPTS[args.opt],
                        precision=sdg.PREC_FP64)
@@ -540,6 +543,10 @@ def bench_serving(sdg, args, rate=None):
         sdg.synchronize()
         pt += time.perf_counter() - tt
         s.close()
+    if cached is not None:
+        pt = cached
+    elif plain_cache is not None:
+        plain_cache["t"] = pt
     sample_dofs = sum((r["p"] + 1) ** 3 * r["NeX"] * r["NeY"] * r["NeZ"] * 3 * r["nstep"]
                       for r in reqs[:k])
     plain_solves = len(reqs) / (pt * dofs / sample_dofs)
@@ -706,10 +713,19 @@ def run_ours(args, ws, rank, local):
     if ws == 1 and not args.no_ensemble:
         line["ensemble"] = bench_ensemble(sdg, args)
     if ws == 1 and not args.no_serving:
-        line["serving"] = bench_serving(sdg, args)
+        plain_cache = {}
+        line["serving"] = bench_serving(sdg, args, plain_cache=plain_cache)
         # the same request stream offered faster than the GPU can serve it:
         # throughput and tail latency of the saturated server
-        line["serving_saturated"] = bench_serving(sdg, args, args.serve_rate_saturated)
+        line["serving_saturated"] = bench_serving(sdg, args, args.serve_rate_saturated,
+                                                  plain_cache)
+        # the offered rate swept across the 10-2000 req/s range
+        line["serving_rate_sweep"] = []
+        for r in (float(x) for x in args.serve_sweep.split(",") if x):
+            res = bench_serving(sdg, args, r, plain_cache)
+            line["serving_rate_sweep"].append(
+                {k: res[k] for k in ("offered_rate_req_s", "solves_per_s", "p50_latency_s",
+                                     "p99_latency_s", "gdof_updates_per_s", "ratio_vs_plain")})
     if ws == 1 and not args.no_sweep:
         line["order_sweep"] = bench_order_sweep(sdg, args)
     print(json.dumps(line), flush=True)
@@ -749,6 +765,8 @@ def main() -> int:
     ap.add_argument("--serve-n", type=int, default=60)
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-rate-saturated", type=float, default=200.0)
+    ap.add_argument("--serve-sweep", default="10,50,100,500,2000",
+                    help="offered rates (req/s) of the serving sweep, comma separated")
     ap.add_argument("--serve-max-ne", type=int, default=32)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     ap.add_argument("--serve-plain-sample", type=int, default=8)
