@@ -328,6 +328,7 @@ def bench_ensemble(sdg, args):
                        [m["dt"] for m in members], ops)
     if args.batch_opt != "evenodd":
         ens.set_opt(OPTS[args.batch_opt])
+    ens.set_parallel_groups(args.parallel_groups)
     for i, m in enumerate(members):
         ens.init_blob(i, m["centre"], m["sigma"], m["vel"])
     sdg.synchronize()
@@ -509,7 +510,7 @@ def bench_serving(sdg, args, rate=None, plain_cache=None):
         t += -math.log(1.0 - rng.uniform()) / (rate or args.serve_rate)
         arrivals.append(t)
     srv = sdg.Server(ops, hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)),
-                     opt=OPTS[args.batch_opt])
+                     opt=OPTS[args.batch_opt], parallel_groups=args.parallel_groups)
     # warm the batched kernel and the pool
     srv.wait(srv.submit(**reqs[0]))
     srv.reset_stats()
@@ -765,6 +766,9 @@ def main() -> int:
     ap.add_argument("--serve-n", type=int, default=60)
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-rate-saturated", type=float, default=200.0)
+    ap.add_argument("--parallel-groups", action="store_true",
+                    help="run the batched forms' order groups on parallel streams instead of "
+                         "one after the other")
     ap.add_argument("--serve-sweep", default="10,50,100,500,2000",
                     help="offered rates (req/s) of the serving sweep, comma separated")
     ap.add_argument("--serve-max-ne", type=int, default=32)

@@ -70,6 +70,10 @@ const char* sdg_status_string(int status);
 const char* sdg_last_error(void);
 /* Library version string. */
 const char* sdg_version(void);
+/* sizeof of a struct of this header by its name ("sdg_server_config",
+ * "sdg_request", "sdg_result", "sdg_server_stats"), 0 for another name: lets
+ * a binding check its struct layouts against the library's. */
+size_t sdg_struct_size(const char* name);
 /* Number of visible CUDA devices (0 when none); never fails. */
 int sdg_device_count(void);
 /* Makes `device` current for the calling host thread (cudaSetDevice). */
@@ -346,7 +350,8 @@ int sdg_solver_destroy(sdg_solver* s);
  * dt) advanced together in FP32-compute / FP64-state form.  A step is a CUDA
  * graph of one persistent launch per RK stage and (order, stage body) group
  * (the blocks of a group take its (instance, element block) work items
- * round-robin) and an index advance: 3 x groups + 1 kernels.
+ * round-robin; the groups run on parallel branches) and an index advance:
+ * 3 x groups + 1 kernels.
  * dims holds NeX,NeY,NeZ per instance; D1D_by_order / Lift_by_order /
  * x1D_by_order are indexed by the order (entries for absent orders may be
  * NULL; x1D_by_order may be NULL when sdg_ensemble_init_blob is not used).
@@ -374,11 +379,22 @@ int sdg_ensemble_set_epb(sdg_ensemble* e, int p, int epb);
  * SDG_OPT_GENERAL / SDG_OPT_OPT1 the node body with running sums.  The
  * choice holds for every order and the autotuner keeps it afterwards. */
 int sdg_ensemble_set_opt(sdg_ensemble* e, int opt);
+/* Block size of every order, or of order p alone. */
 int sdg_ensemble_set_threads(sdg_ensemble* e, int threads);
+int sdg_ensemble_set_order_threads(sdg_ensemble* e, int p, int threads);
+/* threads_by_order receives 12 entries (index = order). */
+int sdg_ensemble_get_threads(const sdg_ensemble* e, int* threads_by_order);
+/* on = 1: the order groups of a step run on parallel graph branches (one
+ * stream each, joined before the index advance); on = 0 (the default): one
+ * after the other on the ensemble's stream.  Results are the same either
+ * way. */
+int sdg_ensemble_set_parallel_groups(sdg_ensemble* e, int on);
 /* eo_by_order receives 12 entries (index = order): 1 where the order's
  * instances run the even-odd body, 0 for the node body or an absent order. */
 int sdg_ensemble_get_bodies(const sdg_ensemble* e, int* eo_by_order);
-/* epb_by_order receives 12 entries (index = order). */
+/* epb_by_order receives 12 entries (index = order); threads the block size
+ * the present orders share (0 when they differ); grid the largest group's
+ * persistent grid. */
 int sdg_ensemble_get_config(const sdg_ensemble* e, int* epb_by_order,
                             int* threads, int* grid);
 int sdg_ensemble_step(sdg_ensemble* e, int nstep);
@@ -405,11 +421,16 @@ typedef struct {
                                90% of the device's free memory) */
   int max_active;           /* requests advanced together at most */
   int max_window_steps;     /* steps between admission points (default 8) */
-  int threads;              /* block size of the batched kernel (0: 256) */
+  int threads;              /* block size of the batched kernels for every
+                               order (0: the default of each order) */
   int epb_by_order[16];     /* elements per block by order (0: default) */
   int opt;                  /* stage body: 0 or SDG_OPT_EVENODD = even-odd where
                                the operators allow it, SDG_OPT_GENERAL /
                                SDG_OPT_OPT1 = node body (running sums) */
+  int threads_by_order[16]; /* block size by order (0: `threads`, else the
+                               default of the order) */
+  int parallel_groups;      /* 0: the order groups of a step run one after the
+                               other on one stream; 1: on parallel streams */
 } sdg_server_config;
 typedef struct {
   int NeX, NeY, NeZ, p, nstep;

@@ -67,20 +67,52 @@ inline void batch_stage_factors(BatchInst& I) {
 struct BatchGroup {
   int p = 0, eo = 0;       // order, 1 for the even-odd body
   int begin = 0, count = 0;  // item range
+  int threads = 256;       // block size
   size_t smem = 0;         // dynamic shared memory of a block
   int grid = 0;            // persistent blocks (resident blocks, at most count)
 };
 
+// Default block size and elements per work item of order p (1..11): the
+// autotuner's choices for the even-odd body on four boxes of about 3.5M DOF
+// of each order, on GB300.
+void batch_default_shape(int p, int* threads, int* epb);
+
 // Sets the group kernel's shared-memory limit and its grid from occupancy.
-int batch_group_setup(BatchGroup& g, int threads);
+int batch_group_setup(BatchGroup& g);
 // Launches stage `stage` (0..2) of one group.
 int batch_group_launch(const BatchInst* d_inst, const BatchItem* d_items, const BatchGroup& g,
-                       int stage, int threads, cudaStream_t st);
-// Splits a sorted item list into groups (epb by order) and sets each up.
+                       int stage, cudaStream_t st);
+// Splits a sorted item list into groups (epb and block size by order) and
+// sets each up.
 int batch_groups(const std::vector<BatchItem>& items, const std::vector<BatchInst>& inst,
-                 const int* epb, int threads, std::vector<BatchGroup>& groups);
+                 const int* epb, const int* threads, std::vector<BatchGroup>& groups);
 // cur = (cur + 1) % 3 for every active instance.
 int batch_advance_launch(BatchInst* d_inst, int n_inst, cudaStream_t st);
+
+// One side stream per order group, when `parallel` is set.  Groups touch
+// disjoint instances, so a step can fork from the caller's stream into the
+// groups' streams (each runs its group's three stages in order) and join
+// them before the index advance, letting a small group's blocks fill the
+// tail of a large group's launch.  Measured on GB300 it is slower (333
+// against 369 solves/s on a 256-member ensemble of orders 3, 5 and 7; 27.4
+// against 28.8 on the saturated serving stream), so the default runs the
+// groups one after the other on the caller's stream.
+struct BatchForkJoin {
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> done;
+  cudaEvent_t fork = nullptr;
+  bool parallel = false;  // false: every group on the caller's stream
+  BatchForkJoin() = default;
+  BatchForkJoin(const BatchForkJoin&) = delete;
+  BatchForkJoin& operator=(const BatchForkJoin&) = delete;
+  ~BatchForkJoin();
+};
+// Enqueues one step of all groups on `st` (forked over the groups when
+// there are several) and the index advance of n_inst instances.  Works
+// under stream capture.
+int batch_step_enqueue(BatchForkJoin& fj, BatchInst* d_inst, int n_inst,
+                       const BatchItem* d_items, const std::vector<BatchGroup>& groups,
+                       cudaStream_t st);
 // Dynamic shared memory the kernel needs for `epb` elements of order p with
 // the node body (eo = 0) or the even-odd body (eo = 1).
 size_t batch_smem_bytes(int p, int epb, int eo);

@@ -204,7 +204,18 @@ int with_group(int p, int eo, F&& f) {
 }
 }  // namespace
 
-int batch_group_setup(BatchGroup& g, int threads) {
+void batch_default_shape(int p, int* threads, int* epb) {
+  // index = order; measured with sdg_ensemble_tune, block sizes 128/256/512
+  static const int kThreads[kBatchMaxOrder + 1] = {256, 128, 128, 128, 128, 128,
+                                                   512, 128, 256, 256, 256, 512};
+  static const int kEpb[kBatchMaxOrder + 1] = {1, 64, 16, 8, 4, 4, 8, 1, 2, 1, 1, 1};
+  const int i = (p >= 1 && p <= kBatchMaxOrder) ? p : 0;
+  *threads = kThreads[i];
+  *epb = kEpb[i];
+}
+
+int batch_group_setup(BatchGroup& g) {
+  const int threads = g.threads;
   int dev = 0, nsm = 0;
   SDG_CUDA_TRY(cudaGetDevice(&dev));
   SDG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -225,16 +236,51 @@ int batch_group_setup(BatchGroup& g, int threads) {
 }
 
 int batch_group_launch(const BatchInst* d_inst, const BatchItem* d_items, const BatchGroup& g,
-                       int stage, int threads, cudaStream_t st) {
+                       int stage, cudaStream_t st) {
   if (g.count <= 0) return SDG_OK;
   return with_group<GroupOps>(g.p, g.eo, [&](auto ops) {
-    return decltype(ops)::launch(d_inst, d_items + g.begin, g.count, stage, g.grid, threads,
+    return decltype(ops)::launch(d_inst, d_items + g.begin, g.count, stage, g.grid, g.threads,
                                  g.smem, st);
   });
 }
 
+BatchForkJoin::~BatchForkJoin() {
+  for (cudaStream_t s : streams) cudaStreamDestroy(s);
+  for (cudaEvent_t e : done) cudaEventDestroy(e);
+  if (fork) cudaEventDestroy(fork);
+}
+
+int batch_step_enqueue(BatchForkJoin& fj, BatchInst* d_inst, int n_inst,
+                       const BatchItem* d_items, const std::vector<BatchGroup>& groups,
+                       cudaStream_t st) {
+  const size_t ng = groups.size();
+  if (ng <= 1 || !fj.parallel) {
+    for (int s = 0; s < 3; s++)
+      for (const BatchGroup& g : groups) SDG_TRY(batch_group_launch(d_inst, d_items, g, s, st));
+    return batch_advance_launch(d_inst, n_inst, st);
+  }
+  if (!fj.fork) SDG_CUDA_TRY(cudaEventCreateWithFlags(&fj.fork, cudaEventDisableTiming));
+  while (fj.streams.size() < ng) {
+    cudaStream_t s;
+    cudaEvent_t e;
+    SDG_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    fj.streams.push_back(s);
+    SDG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    fj.done.push_back(e);
+  }
+  SDG_CUDA_TRY(cudaEventRecord(fj.fork, st));
+  for (size_t i = 0; i < ng; i++) {
+    SDG_CUDA_TRY(cudaStreamWaitEvent(fj.streams[i], fj.fork, 0));
+    for (int s = 0; s < 3; s++)
+      SDG_TRY(batch_group_launch(d_inst, d_items, groups[i], s, fj.streams[i]));
+    SDG_CUDA_TRY(cudaEventRecord(fj.done[i], fj.streams[i]));
+    SDG_CUDA_TRY(cudaStreamWaitEvent(st, fj.done[i], 0));
+  }
+  return batch_advance_launch(d_inst, n_inst, st);
+}
+
 int batch_groups(const std::vector<BatchItem>& items, const std::vector<BatchInst>& inst,
-                 const int* epb, int threads, std::vector<BatchGroup>& groups) {
+                 const int* epb, const int* threads, std::vector<BatchGroup>& groups) {
   groups.clear();
   for (size_t i = 0; i < items.size();) {
     const BatchInst& I = inst[items[i].inst];
@@ -246,9 +292,10 @@ int batch_groups(const std::vector<BatchItem>& items, const std::vector<BatchIns
     while (j < items.size() && inst[items[j].inst].p == g.p && inst[items[j].inst].eo == g.eo)
       j++;
     g.count = (int)(j - i);
+    g.threads = threads[g.p];
     g.smem = batch_smem_bytes(g.p, epb[g.p], g.eo);
     g.grid = 0;
-    SDG_TRY(batch_group_setup(g, threads));
+    SDG_TRY(batch_group_setup(g));
     groups.push_back(g);
     i = j;
   }

@@ -26,21 +26,15 @@ struct sdg_ensemble {
   bool body_fixed = false;         // set_opt chose the body; the tuner keeps it
   double* d_x1D[kBatchMaxOrder + 1] = {};
   int epb[kBatchMaxOrder + 1] = {};
-  int threads = 256;
+  int threads[kBatchMaxOrder + 1] = {};
   std::vector<BatchGroup> groups;  // one persistent launch per order present
+  BatchForkJoin fj;                // a side stream per group
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   long long total_dof = 0;
 };
 
 namespace {
-
-// Default elements per block: about 512 nodes per block.
-int default_epb(int p) {
-  const int np = (p + 1) * (p + 1) * (p + 1);
-  int e = 512 / np;
-  return e < 1 ? 1 : e;
-}
 
 void free_ensemble(sdg_ensemble* e) {
   if (e->graph) cudaGraphExecDestroy(e->graph);
@@ -83,10 +77,7 @@ int build_items(sdg_ensemble* e, const std::vector<int>* subset = nullptr) {
 }
 
 int enqueue_step(sdg_ensemble* e) {
-  for (int s = 0; s < 3; s++)
-    for (const BatchGroup& g : e->groups)
-      SDG_TRY(batch_group_launch(e->d_inst, e->d_items, g, s, e->threads, e->stream));
-  return batch_advance_launch(e->d_inst, e->n, e->stream);
+  return batch_step_enqueue(e->fj, e->d_inst, e->n, e->d_items, e->groups, e->stream);
 }
 
 int capture_graph(sdg_ensemble* e) {
@@ -126,7 +117,7 @@ int time_stage0(sdg_ensemble* e, float* ms) {
     // stage 0 reads q[cur] and writes q[cur+1]: repeating it leaves the state
     SDG_CUDA_TRY(cudaEventRecord(a, e->stream));
     for (const BatchGroup& g : e->groups)
-      SDG_TRY(batch_group_launch(e->d_inst, e->d_items, g, 0, e->threads, e->stream));
+      SDG_TRY(batch_group_launch(e->d_inst, e->d_items, g, 0, e->stream));
     SDG_CUDA_TRY(cudaEventRecord(b, e->stream));
     SDG_CUDA_TRY(cudaEventSynchronize(b));
     float t = 0.f;
@@ -167,7 +158,7 @@ int sdg_ensemble_create(sdg_ensemble** out, int n, const int* dims, const int* o
   e->stream = as_stream(stream);
   e->inst.resize(n);
   e->cur_host.assign(n, 0);
-  for (int p = 0; p <= kBatchMaxOrder; p++) e->epb[p] = default_epb(p);
+  for (int p = 0; p <= kBatchMaxOrder; p++) batch_default_shape(p, &e->threads[p], &e->epb[p]);
   auto bail = [&](int st) {
     free_ensemble(e);
     delete e;
@@ -285,7 +276,19 @@ int sdg_ensemble_set_epb(sdg_ensemble* e, int p, int epb) {
 int sdg_ensemble_set_threads(sdg_ensemble* e, int threads) {
   if (!e || threads < 32 || threads > kBatchThreadsMax || threads % 32)
     return fail(SDG_ERR_INVALID_ARG, "bad block size %d", threads);
-  e->threads = threads;
+  for (int p = 0; p <= kBatchMaxOrder; p++) e->threads[p] = threads;
+  if (e->graph) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  return build_items(e);
+}
+
+int sdg_ensemble_set_order_threads(sdg_ensemble* e, int p, int threads) {
+  if (!e || p < 1 || p > kBatchMaxOrder || threads < 32 || threads > kBatchThreadsMax ||
+      threads % 32)
+    return fail(SDG_ERR_INVALID_ARG, "bad block size %d for order %d", threads, p);
+  e->threads[p] = threads;
   if (e->graph) {
     cudaGraphExecDestroy(e->graph);
     e->graph = nullptr;
@@ -316,6 +319,22 @@ int sdg_ensemble_set_opt(sdg_ensemble* e, int opt) {
   return build_items(e);
 }
 
+int sdg_ensemble_set_parallel_groups(sdg_ensemble* e, int on) {
+  if (!e) return fail(SDG_ERR_INVALID_ARG, "NULL ensemble");
+  e->fj.parallel = (on != 0);
+  if (e->graph) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  return SDG_OK;
+}
+
+int sdg_ensemble_get_threads(const sdg_ensemble* e, int* threads_by_order) {
+  if (!e || !threads_by_order) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  for (int p = 0; p <= kBatchMaxOrder; p++) threads_by_order[p] = e->threads[p];
+  return SDG_OK;
+}
+
 int sdg_ensemble_get_bodies(const sdg_ensemble* e, int* eo_by_order) {
   if (!e || !eo_by_order) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
   for (int p = 0; p <= kBatchMaxOrder; p++) {
@@ -330,7 +349,15 @@ int sdg_ensemble_get_config(const sdg_ensemble* e, int* epb_by_order, int* threa
   if (!e) return fail(SDG_ERR_INVALID_ARG, "NULL ensemble");
   if (epb_by_order)
     for (int p = 0; p <= kBatchMaxOrder; p++) epb_by_order[p] = e->epb[p];
-  if (threads) *threads = e->threads;
+  if (threads) {
+    // the block size the present orders share, or 0 when they differ
+    *threads = -1;
+    for (int i = 0; i < e->n; i++) {
+      const int t = e->threads[e->inst[i].p];
+      *threads = (*threads == -1 || *threads == t) ? t : 0;
+    }
+    if (*threads < 0) *threads = 0;
+  }
   if (grid) {
     *grid = 0;
     for (const BatchGroup& g : e->groups) *grid = std::max(*grid, g.grid);
@@ -340,45 +367,29 @@ int sdg_ensemble_get_config(const sdg_ensemble* e, int* epb_by_order, int* threa
 
 // Autotuner: for each order present, time stage 0 over that order's
 // instances for both stage bodies (even-odd where the operators allow it, and
-// the node body) and every elements-per-block candidate (about 64 to 4096
-// nodes a block, shared memory under 96 KB) at each block size in
-// {128, 256, 512}; keep per order the fastest body and candidate, then keep
-// the block size whose summed best times are smallest.  After set_opt the
-// body stays the one it chose.  Stage 0 leaves the state unchanged, so tuning can
-// run at any point.
+// the node body; after set_opt only the body it chose), each block size in
+// {128, 256, 512} and every elements-per-block candidate (about 64 to 4096
+// nodes a block, shared memory under 96 KB), and keep the fastest
+// (body, block size, elements per block) of each order.  Stage 0 leaves the
+// state unchanged, so tuning can run at any point.
 int sdg_ensemble_tune(sdg_ensemble* e) {
   if (!e) return fail(SDG_ERR_INVALID_ARG, "NULL ensemble");
   std::vector<std::vector<int>> by_order(kBatchMaxOrder + 1);
   for (int i = 0; i < e->n; i++) by_order[e->inst[i].p].push_back(i);
   const int thread_opts[3] = {128, 256, 512};
-  double best_total = 1e300;
-  int best_threads = e->threads;
-  int best_epb[kBatchMaxOrder + 1];
-  for (int p = 0; p <= kBatchMaxOrder; p++) best_epb[p] = e->epb[p];
-  const int saved_threads = e->threads;
-  int saved_epb[kBatchMaxOrder + 1], saved_eo[kBatchMaxOrder + 1], best_eo[kBatchMaxOrder + 1];
-  for (int p = 0; p <= kBatchMaxOrder; p++) {
-    saved_epb[p] = e->epb[p];
-    saved_eo[p] = best_eo[p] = e->eo_by_order[p];
-  }
-  for (int th : thread_opts) {
-    e->threads = th;
-    double total = 0;
-    int epb_here[kBatchMaxOrder + 1], eo_here[kBatchMaxOrder + 1];
-    for (int p = 0; p <= kBatchMaxOrder; p++) {
-      epb_here[p] = e->epb[p];
-      eo_here[p] = saved_eo[p];
-    }
-    for (int p = 1; p <= kBatchMaxOrder; p++) {
-      if (by_order[p].empty()) continue;
-      const int np = (p + 1) * (p + 1) * (p + 1);
-      float best = 1e30f;
-      const bool has_eo = e->inst[by_order[p][0]].eo_tab != nullptr;
-      const int body_hi = e->body_fixed ? saved_eo[p] : (has_eo ? 1 : 0);
-      const int body_lo = e->body_fixed ? saved_eo[p] : 0;
-      for (int body = body_hi; body >= body_lo; body--) {
-        e->eo_by_order[p] = body;
-        set_bodies(e);
+  for (int p = 1; p <= kBatchMaxOrder; p++) {
+    if (by_order[p].empty()) continue;
+    const int np = (p + 1) * (p + 1) * (p + 1);
+    const bool has_eo = e->inst[by_order[p][0]].eo_tab != nullptr;
+    const int body_hi = e->body_fixed ? e->eo_by_order[p] : (has_eo ? 1 : 0);
+    const int body_lo = e->body_fixed ? e->eo_by_order[p] : 0;
+    float best = 1e30f;
+    int best_eo = e->eo_by_order[p], best_th = e->threads[p], best_epb = e->epb[p];
+    for (int body = body_hi; body >= body_lo; body--) {
+      e->eo_by_order[p] = body;
+      set_bodies(e);
+      for (int th : thread_opts) {
+        e->threads[p] = th;
         for (int cand = 1; cand <= 256; cand *= 2) {
           if (cand * np > 4096 || (cand * np < 64 && cand * 2 * np <= 4096)) continue;
           if (batch_smem_bytes(p, cand, body) > 96 * 1024) continue;
@@ -388,35 +399,18 @@ int sdg_ensemble_tune(sdg_ensemble* e) {
           SDG_TRY(time_stage0(e, &ms));
           if (ms < best) {
             best = ms;
-            epb_here[p] = cand;
-            eo_here[p] = body;
+            best_eo = body;
+            best_th = th;
+            best_epb = cand;
           }
         }
       }
-      e->epb[p] = epb_here[p];
-      total += best;
     }
-    if (total < best_total) {
-      best_total = total;
-      best_threads = th;
-      for (int p = 0; p <= kBatchMaxOrder; p++) {
-        best_epb[p] = epb_here[p];
-        best_eo[p] = eo_here[p];
-      }
-    }
-    for (int p = 0; p <= kBatchMaxOrder; p++) {
-      e->epb[p] = saved_epb[p];
-      e->eo_by_order[p] = saved_eo[p];
-    }
+    e->eo_by_order[p] = best_eo;
+    e->threads[p] = best_th;
+    e->epb[p] = best_epb;
     set_bodies(e);
   }
-  (void)saved_threads;
-  e->threads = best_threads;
-  for (int p = 0; p <= kBatchMaxOrder; p++) {
-    e->epb[p] = best_epb[p];
-    e->eo_by_order[p] = best_eo[p];
-  }
-  set_bodies(e);
   if (e->graph) {
     cudaGraphExecDestroy(e->graph);
     e->graph = nullptr;

@@ -261,6 +261,16 @@ const char* sdg_last_error(void) { return g_last_error.c_str(); }
 
 const char* sdg_version(void) { return "sdg_gb300 0.1 (sm_103a)"; }
 
+size_t sdg_struct_size(const char* name) {
+  if (!name) return 0;
+  const std::string n(name);
+  if (n == "sdg_server_config") return sizeof(sdg_server_config);
+  if (n == "sdg_request") return sizeof(sdg_request);
+  if (n == "sdg_result") return sizeof(sdg_result);
+  if (n == "sdg_server_stats") return sizeof(sdg_server_stats);
+  return 0;
+}
+
 int sdg_device_count(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) {

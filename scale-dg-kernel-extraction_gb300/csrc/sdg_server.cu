@@ -69,7 +69,8 @@ struct sdg_server {
   int d_items_cap = 0;
   int n_items = 0;
   std::vector<BatchGroup> groups;  // one persistent launch per order active
-  int threads = 256;
+  BatchForkJoin fj;                // a side stream per group
+  int threads[kBatchMaxOrder + 1] = {};
   int epb[kBatchMaxOrder + 1] = {};
   // statistics
   std::vector<double> latencies;
@@ -168,10 +169,7 @@ int rebuild_tables(sdg_server* s) {
 int run_steps(sdg_server* s, int nsteps) {
   const int n = (int)s->active.size();
   for (int k = 0; k < nsteps; k++) {
-    for (int st = 0; st < 3; st++)
-      for (const BatchGroup& g : s->groups)
-        SDG_TRY(batch_group_launch(s->d_inst, s->d_items, g, st, s->threads, s->stream));
-    SDG_TRY(batch_advance_launch(s->d_inst, n, s->stream));
+    SDG_TRY(batch_step_enqueue(s->fj, s->d_inst, n, s->d_items, s->groups, s->stream));
     s->launches += 3 * (long long)s->groups.size() + 1;
   }
   return SDG_OK;
@@ -312,14 +310,20 @@ int sdg_server_create(sdg_server** out, const sdg_server_config* cfg,
   if (cfg->opt != 0 && cfg->opt != SDG_OPT_GENERAL && cfg->opt != SDG_OPT_OPT1 &&
       cfg->opt != SDG_OPT_EVENODD)
     return fail(SDG_ERR_BAD_OPTTYPE, "unknown opt type %d", cfg->opt);
+  for (int p = -1; p < 16; p++) {
+    const int t = p < 0 ? cfg->threads : cfg->threads_by_order[p];
+    if (t != 0 && (t < 32 || t > kBatchThreadsMax || t % 32))
+      return fail(SDG_ERR_INVALID_ARG, "bad block size %d", t);
+  }
   SDG_TRY(require_device());
   sdg_server* s = new (std::nothrow) sdg_server();
   if (!s) return fail(SDG_ERR_OUT_OF_MEMORY, "host allocation failed");
   s->cfg = *cfg;
-  if (s->cfg.threads > 0) s->threads = s->cfg.threads;
+  s->fj.parallel = (cfg->parallel_groups != 0);
   for (int p = 0; p <= kBatchMaxOrder; p++) {
-    const int np = (p + 1) * (p + 1) * (p + 1);
-    s->epb[p] = std::max(1, 512 / np);
+    batch_default_shape(p, &s->threads[p], &s->epb[p]);
+    if (cfg->threads > 0) s->threads[p] = cfg->threads;
+    if (cfg->threads_by_order[p] > 0) s->threads[p] = cfg->threads_by_order[p];
     if (cfg->epb_by_order[p] > 0) s->epb[p] = cfg->epb_by_order[p];
   }
   auto bail = [&](int st) {

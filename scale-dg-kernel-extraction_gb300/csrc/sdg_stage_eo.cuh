@@ -78,8 +78,8 @@ struct EoCfg {
 // direction tables, then per element q, F_x (later the line-result sums), F_y,
 // F_z and the 6 Nfp face fluxes, then the neighbour indices.
 // The FP64 body does not stage q: the face flux and the RK update read it
-// from global memory (L1 / L2 hits after phase 0), which leaves room for a
-// third resident block.
+// from global memory (L1 / L2 hits after phase 0), which saves shared memory
+// for a fourth resident block.
 template <typename CT>
 __host__ __device__ constexpr bool eo_stages_q() {
   return sizeof(CT) == 4;
@@ -136,7 +136,7 @@ __device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, C
   const CT gs = gm + gp, gd = gm - gp;
   // rows unrolled up to p = 7 in FP32 and p = 4 in FP64; above that a rolled
   // loop keeps the 2H line values and the row sums within the register budget
-  // (85 registers for three resident FP64 blocks)
+  // (64 registers for four resident FP64 blocks of 256 threads)
   constexpr int kRowUnroll = (N <= (sizeof(CT) == 8 ? 5 : 8)) ? RPP : 1;
 #pragma unroll kRowUnroll
   for (int ii = 0; ii < RPP; ii++) {
@@ -363,10 +363,11 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   });
 }
 
-// Three resident blocks an SM.  FP32 (512 threads, registers capped at 42):
-// the body issues few instructions per byte and needs the warps to hide
-// memory latency.  FP64 (256 threads, 85 registers): a block in its load or
-// flux phase leaves two others feeding the FP64 pipe.
+// FP32: three resident blocks of 512 threads (registers capped at 42): the
+// body issues few instructions per byte and needs the warps to hide memory
+// latency.  FP64: four resident blocks of 256 threads (registers capped at
+// 64): a block in its load or flux phase leaves three others feeding the
+// FP64 pipe.
 template <int P, typename CT>
 __global__ void __launch_bounds__(EoCfg<P, CT>::THREADS, sizeof(CT) == 8 ? 4 : 3)
     stage_eo_kernel(const StageArgs a) {

@@ -41,7 +41,8 @@ PREC_FP64_EMU = 2
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_size_t), ("max_active", C.c_int),
                 ("max_window_steps", C.c_int), ("threads", C.c_int),
-                ("epb_by_order", C.c_int * 16), ("opt", C.c_int)]
+                ("epb_by_order", C.c_int * 16), ("opt", C.c_int),
+                ("threads_by_order", C.c_int * 16), ("parallel_groups", C.c_int)]
 
 
 class Request(C.Structure):
@@ -86,6 +87,7 @@ def _load() -> C.CDLL:
         "sdg_status_string": ([_i], C.c_char_p),
         "sdg_last_error": ([], C.c_char_p),
         "sdg_version": ([], C.c_char_p),
+        "sdg_struct_size": ([C.c_char_p], C.c_size_t),
         "sdg_device_count": ([], _i),
         "sdg_device_synchronize": ([], _i),
         "sdg_set_device": ([_i], _i),
@@ -145,6 +147,9 @@ def _load() -> C.CDLL:
         "sdg_ensemble_set_epb": ([_vp, _i, _i], _i),
         "sdg_ensemble_set_opt": ([_vp, _i], _i),
         "sdg_ensemble_set_threads": ([_vp, _i], _i),
+        "sdg_ensemble_set_order_threads": ([_vp, _i, _i], _i),
+        "sdg_ensemble_get_threads": ([_vp, _ip], _i),
+        "sdg_ensemble_set_parallel_groups": ([_vp, _i], _i),
         "sdg_ensemble_get_config": ([_vp, _ip, C.POINTER(_i), C.POINTER(_i)], _i),
         "sdg_ensemble_get_bodies": ([_vp, _ip], _i),
         "sdg_ensemble_step": ([_vp, _i], _i),
@@ -520,8 +525,18 @@ class Ensemble:
     def set_epb(self, p, epb) -> None:
         _check(lib.sdg_ensemble_set_epb(self._h, p, epb), "sdg_ensemble_set_epb")
 
-    def set_threads(self, threads) -> None:
-        _check(lib.sdg_ensemble_set_threads(self._h, threads), "sdg_ensemble_set_threads")
+    def set_threads(self, threads, p=None) -> None:
+        """Block size of every order, or of order p alone."""
+        if p is None:
+            _check(lib.sdg_ensemble_set_threads(self._h, threads), "sdg_ensemble_set_threads")
+        else:
+            _check(lib.sdg_ensemble_set_order_threads(self._h, p, threads),
+                   "sdg_ensemble_set_order_threads")
+
+    def set_parallel_groups(self, on: bool) -> None:
+        """Order groups on parallel graph branches (True) or one stream."""
+        _check(lib.sdg_ensemble_set_parallel_groups(self._h, int(bool(on))),
+               "sdg_ensemble_set_parallel_groups")
 
     def launches_per_step(self) -> int:
         return lib.sdg_ensemble_launches_per_step(self._h)
@@ -537,9 +552,12 @@ class Ensemble:
                "sdg_ensemble_get_config")
         eo = np.zeros(12, dtype=np.int32)
         _check(lib.sdg_ensemble_get_bodies(self._h, eo), "sdg_ensemble_get_bodies")
+        tb = np.zeros(12, dtype=np.int32)
+        _check(lib.sdg_ensemble_get_threads(self._h, tb), "sdg_ensemble_get_threads")
         orders = sorted(set(self.orders))
         return {"epb": {p: int(epb[p]) for p in orders},
                 "body": {p: ("evenodd" if eo[p] else "node") for p in orders},
+                "threads_by_order": {p: int(tb[p]) for p in orders},
                 "threads": th.value, "grid": gr.value}
 
     def step(self, nstep: int) -> None:
@@ -585,7 +603,10 @@ class Server:
     """Continuous-batching solve server (sdg_server_* in include/sdg_advect.h)."""
 
     def __init__(self, ops_by_order, hbm_budget_bytes=64 << 30, max_active=512,
-                 max_window_steps=8, threads=0, device=0, opt=0):
+                 max_window_steps=8, threads=0, device=0, opt=0, threads_by_order=None,
+                 epb_by_order=None, parallel_groups=False):
+        """threads_by_order / epb_by_order: {p: value} overrides of the
+        batched kernels' launch shape (results do not depend on it)."""
         self._arrs, D, L, X = _order_table(ops_by_order)
         cfg = ServerConfig()
         cfg.device = device
@@ -594,6 +615,11 @@ class Server:
         cfg.max_active = max_active
         cfg.max_window_steps = max_window_steps
         cfg.threads = threads
+        cfg.parallel_groups = 1 if parallel_groups else 0
+        for p, t in (threads_by_order or {}).items():
+            cfg.threads_by_order[p] = t
+        for p, e in (epb_by_order or {}).items():
+            cfg.epb_by_order[p] = e
         self._h = _vp()
         _check(lib.sdg_server_create(C.byref(self._h), C.byref(cfg), C.cast(D, C.POINTER(_vp)),
                                      C.cast(L, C.POINTER(_vp)), C.cast(X, C.POINTER(_vp))),

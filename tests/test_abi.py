@@ -38,6 +38,16 @@ def test_header_compiles_as_c(tmp_path):
     assert r == 0
 
 
+def test_binding_struct_layouts_match_the_library():
+    lib = ctypes.CDLL(sdg.LIB_PATH)
+    lib.sdg_struct_size.argtypes = [ctypes.c_char_p]
+    lib.sdg_struct_size.restype = ctypes.c_size_t
+    for name, cls in (("sdg_server_config", sdg.ServerConfig), ("sdg_request", sdg.Request),
+                      ("sdg_result", sdg.Result), ("sdg_server_stats", sdg.ServerStats)):
+        assert lib.sdg_struct_size(name.encode()) == ctypes.sizeof(cls), name
+    assert lib.sdg_struct_size(b"no_such_struct") == 0
+
+
 def test_status_strings():
     assert sdg.status_string(sdg.OK) == "ok"
     for st in range(-9, 0):

@@ -86,7 +86,8 @@ def test_autotuner_keeps_results_and_picks_valid_shapes():
     ens, fields, dts, ops = build(MEMBERS, seed0=300)
     assert all(b == "evenodd" for b in ens.config()["body"].values())
     cfg = ens.tune()
-    assert cfg["threads"] in (128, 256, 512) and cfg["grid"] > 0
+    assert cfg["threads"] in (0, 128, 256, 512) and cfg["grid"] > 0
+    assert set(cfg["threads_by_order"].values()) <= {128, 256, 512}
     assert set(cfg["body"]) == {p for _, p in MEMBERS}
     for p, e in cfg["epb"].items():
         assert e >= 1
@@ -107,6 +108,32 @@ def test_set_opt_overrides_the_tuned_bodies_and_the_tuner_keeps_it():
     for i, (dims, p) in enumerate(MEMBERS[:4]):
         want = standalone(dims, p, fields[i], dts[i], ops, 2, sdg.OPT_GENERAL)
         assert np.array_equal(ens.download(i), want), i
+
+
+def test_block_size_per_order_keeps_results():
+    ens, fields, dts, ops = build(MEMBERS, seed0=450)
+    ens.set_threads(512)
+    ens.set_threads(128, p=7)
+    ens.set_threads(256, p=3)
+    cfg = ens.config()
+    assert cfg["threads"] == 0
+    assert cfg["threads_by_order"][7] == 128 and cfg["threads_by_order"][3] == 256
+    assert cfg["threads_by_order"][11] == 512
+    ens.step(3)
+    for i, (dims, p) in enumerate(MEMBERS):
+        want = standalone(dims, p, fields[i], dts[i], ops, 3)
+        assert np.array_equal(ens.download(i), want), (i, p)
+
+
+def test_parallel_group_branches_keep_results():
+    ens, fields, dts, ops = build(MEMBERS, seed0=470)
+    ens.set_parallel_groups(True)
+    ens.step(2)
+    ens.set_parallel_groups(False)
+    ens.step(1)
+    for i, (dims, p) in enumerate(MEMBERS):
+        want = standalone(dims, p, fields[i], dts[i], ops, 3)
+        assert np.array_equal(ens.download(i), want), (i, p)
 
 
 def test_explicit_shapes_and_graph_replay_compose():

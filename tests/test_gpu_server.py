@@ -70,6 +70,29 @@ def test_result_is_the_same_alone_and_in_the_mix(ops, body):
     srv.close()
 
 
+def test_launch_shape_does_not_change_results(ops):
+    rs = [req((3, 4, 2), 5, 12, 41), req((2, 3, 3), 2, 9, 42), req((2, 2, 3), 11, 7, 43),
+          req((4, 2, 2), 7, 10, 44)]
+    outs = []
+    for kw in ({}, dict(threads=512), dict(parallel_groups=True),
+               dict(threads_by_order={2: 128, 5: 512, 7: 256, 11: 128},
+                    epb_by_order={2: 4, 5: 1, 7: 2})):
+        srv = sdg.Server(ops, **kw)
+        tks = [srv.submit(**r, want_state=True) for r in rs]
+        outs.append([srv.wait(t)[1] for t in tks])
+        assert srv.stats()["fatal_status"] == 0
+        srv.close()
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a, b)
+
+
+def test_bad_server_block_size_is_rejected(ops):
+    with pytest.raises(sdg.SdgError) as e:
+        sdg.Server(ops, threads_by_order={5: 100})
+    assert e.value.status == sdg.ERR_INVALID_ARG
+
+
 @pytest.mark.parametrize("opt", [0, sdg.OPT_GENERAL])
 def test_served_result_matches_fp64_oracle_within_fp32_tolerance(ops, opt):
     r = req((3, 2, 3), 3, 20, 31)
