@@ -18,15 +18,25 @@ static_assert(kInstWords < 128, "the smallest block must copy the header in one 
 // One persistent launch runs the items of one order group (order P, stage
 // body EO: 1 even-odd, 0 node body; RK the stage's update kind).  Compiling
 // one order and one body per kernel keeps each at its own register count
-// (40 for 3 blocks of 512 threads an SM), where a switch over the orders
-// would keep the union of their needs.
+// (32 or 40, for 4 or 3 blocks of 512 threads an SM), where a switch over
+// the orders would keep the union of their needs.
 //
 // Items are assigned round-robin (block b runs items b, b + G, b + 2G, ...).
 // The next item's instance header is fetched into shared memory while the
 // current item computes, and the item after that into a register, so that a
 // block never waits on the item -> instance -> data chain of dependent loads.
+// Resident blocks of 512 threads an SM the registers are capped for: 4 (32
+// registers) where that measured faster on GB300, else 3 (40 registers).
+// The node body gains 4-16 % from the fourth block at every order; the
+// even-odd body at p = 1, 5, 7, 8, 9 and 11 (up to 22 % at p = 11) and loses
+// up to 10 % at p = 2, 3, 4, 6 and 10, where the cap spills.
+template <int P, int EO>
+__host__ __device__ constexpr int batch_min_blocks() {
+  return (EO == 0 || P == 1 || P == 5 || P == 7 || P == 8 || P == 9 || P == 11) ? 4 : 3;
+}
+
 template <int P, int EO, int RK>
-__global__ void __launch_bounds__(kBatchThreadsMax, 3)
+__global__ void __launch_bounds__(kBatchThreadsMax, batch_min_blocks<P, EO>())
     batch_order_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
                        int n_items, int stage) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -206,9 +216,9 @@ int with_group(int p, int eo, F&& f) {
 
 void batch_default_shape(int p, int* threads, int* epb) {
   // index = order; measured with sdg_ensemble_tune, block sizes 128/256/512
-  static const int kThreads[kBatchMaxOrder + 1] = {256, 128, 128, 128, 128, 128,
-                                                   512, 128, 256, 256, 256, 512};
-  static const int kEpb[kBatchMaxOrder + 1] = {1, 64, 16, 8, 4, 4, 8, 1, 2, 1, 1, 1};
+  static const int kThreads[kBatchMaxOrder + 1] = {256, 128, 128, 128, 128, 256,
+                                                   512, 512, 512, 256, 256, 512};
+  static const int kEpb[kBatchMaxOrder + 1] = {1, 64, 16, 8, 4, 4, 8, 4, 2, 1, 1, 1};
   const int i = (p >= 1 && p <= kBatchMaxOrder) ? p : 0;
   *threads = kThreads[i];
   *epb = kEpb[i];

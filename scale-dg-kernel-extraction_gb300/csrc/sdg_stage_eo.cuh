@@ -363,13 +363,20 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   });
 }
 
-// FP32: three resident blocks of 512 threads (registers capped at 42): the
-// body issues few instructions per byte and needs the warps to hide memory
-// latency.  FP64: four resident blocks of 256 threads (registers capped at
-// 64): a block in its load or flux phase leaves three others feeding the
-// FP64 pipe.
+// Resident blocks an SM.  FP32 (512 threads): the body issues few
+// instructions per byte and needs warps to hide memory latency, so up to
+// p = 12 the registers are capped at 32 for four blocks (64 warps; measured
+// 1.0-1.16x the three-block build, 100 against 91.5 GDOF-updates/s at p = 7);
+// above that shared memory admits three and the cap would only spill.
+// FP64: four blocks of 256 threads (registers capped at 64): a block in its
+// load or flux phase leaves three others feeding the FP64 pipe.
 template <int P, typename CT>
-__global__ void __launch_bounds__(EoCfg<P, CT>::THREADS, sizeof(CT) == 8 ? 4 : 3)
+__host__ __device__ constexpr int eo_min_blocks() {
+  return sizeof(CT) == 8 ? 4 : (P <= 12 ? 4 : 3);
+}
+
+template <int P, typename CT>
+__global__ void __launch_bounds__(EoCfg<P, CT>::THREADS, eo_min_blocks<P, CT>())
     stage_eo_kernel(const StageArgs a) {
   constexpr int EPB = EoCfg<P, CT>::EPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
