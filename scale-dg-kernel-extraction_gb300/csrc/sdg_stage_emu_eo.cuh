@@ -149,8 +149,18 @@ __device__ __forceinline__ void emu_eo_line(const float2* row, const float2* __r
   }
 }
 
+// Resident blocks of 256 threads an SM the registers are capped for.  The
+// body waits on both the FP64 pipe and instruction issue, and more warps
+// overlap the two: measured on GB300, six blocks (40 registers) up to p = 6
+// and five (48 registers, no spills) up to p = 12 run 1.07-1.14x four blocks;
+// above p = 12 the caps spill and four blocks are faster.
 template <int P>
-__global__ void __launch_bounds__(EmuEoCfg<P>::THREADS, 4)
+__host__ __device__ constexpr int emu_eo_min_blocks() {
+  return P <= 6 ? 6 : (P <= 12 ? 5 : 4);
+}
+
+template <int P>
+__global__ void __launch_bounds__(EmuEoCfg<P>::THREADS, emu_eo_min_blocks<P>())
     stage_emu_eo_kernel(const StageArgs a) {
   using O = Ord<P>;
   using Sh = EoShape<P>;
