@@ -520,12 +520,20 @@ int sdg_solver_solve_host_pipelined(sdg_solver* s, int count, const double* cons
   SDG_CUDA_TRY(cudaEventRecord(start, s->stream));
   SDG_CUDA_TRY(cudaStreamWaitEvent(s->h2d, start, 0));
   cudaEventDestroy(start);
+  // A request's result ends in state buffer nstep % 3.  The uploads write
+  // buffer 0 (and, in FP32, stage the velocity through a buffer that is not
+  // the result), so they wait for the slot's previous download only when the
+  // result sits in buffer 0; the compute of a request waits for it always,
+  // since the RK stages write every buffer.  The next upload thus overlaps the
+  // previous download instead of queueing behind it.
+  const int out_buf = nstep % 3;
+  const int stage_buf = (out_buf == 1) ? 2 : 1;
   for (int r = 0; r < count; r++) {
     IoSlot& io = s->io[r % 2];
     if (r >= 2) {
-      // the slot's previous request must have finished reading and downloading
+      // the slot's previous request must have finished reading its inputs
       SDG_CUDA_TRY(cudaStreamWaitEvent(s->h2d, io.computed, 0));
-      SDG_CUDA_TRY(cudaStreamWaitEvent(s->h2d, io.downloaded, 0));
+      if (out_buf == 0) SDG_CUDA_TRY(cudaStreamWaitEvent(s->h2d, io.downloaded, 0));
     }
     SDG_CUDA_TRY(cudaMemcpyAsync(io.q[0], q_in[r], bytes, cudaMemcpyHostToDevice, s->h2d));
     const double* src[3] = {u[r], v[r], w[r]};
@@ -535,14 +543,16 @@ int sdg_solver_solve_host_pipelined(sdg_solver* s, int count, const double* cons
         SDG_CUDA_TRY(cudaMemcpyAsync(dst[c], src[c], bytes, cudaMemcpyHostToDevice, s->h2d));
       } else {
         // FP64 staging through a free state buffer, narrowed on the device
-        SDG_CUDA_TRY(cudaMemcpyAsync(io.q[1], src[c], bytes, cudaMemcpyHostToDevice, s->h2d));
+        SDG_CUDA_TRY(cudaMemcpyAsync(io.q[stage_buf], src[c], bytes, cudaMemcpyHostToDevice,
+                                     s->h2d));
         f64_to_f32_kernel<<<grid_for(s->ndof), 256, 0, s->h2d>>>(static_cast<float*>(dst[c]),
-                                                               io.q[1], s->ndof);
+                                                               io.q[stage_buf], s->ndof);
         SDG_CUDA_TRY(cudaGetLastError());
       }
     }
     SDG_CUDA_TRY(cudaEventRecord(io.uploaded, s->h2d));
     SDG_CUDA_TRY(cudaStreamWaitEvent(s->comp, io.uploaded, 0));
+    if (r >= 2) SDG_CUDA_TRY(cudaStreamWaitEvent(s->comp, io.downloaded, 0));
     int cur = 0;
     for (int it = 0; it < nstep; it++) {
       const int s0 = cur, s1 = (cur + 1) % 3, s2 = (cur + 2) % 3;

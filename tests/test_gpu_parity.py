@@ -136,8 +136,11 @@ def test_fp32_evenodd_tendency(p):
 
 
 @pytest.mark.parametrize("prec", [sdg.PREC_FP64, sdg.PREC_FP32, sdg.PREC_FP64_EMU])
-def test_pipelined_host_solves_equal_plain_solves(prec):
-    dims, p, nstep = (3, 2, 4), 5, 3
+@pytest.mark.parametrize("nstep", [1, 2, 3])
+def test_pipelined_host_solves_equal_plain_solves(prec, nstep):
+    """Every result buffer (nstep % 3) and so every wait pattern of the
+    two-slot pipeline; boxes large enough that copies overlap compute."""
+    dims, p = (12, 10, 8), 5
     cases = [Case(*dims, p, ic="blob", seed=W.BASE_SEED + 60 + r) for r in range(5)]
     n = cases[0].nown
     pins = [[sdg.PinnedArray(n) for _ in range(5)] for _ in cases]
