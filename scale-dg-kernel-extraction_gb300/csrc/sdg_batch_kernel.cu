@@ -35,6 +35,14 @@ __host__ __device__ constexpr int batch_min_blocks() {
   return (EO == 0 || P == 1 || P == 5 || P == 7 || P == 8 || P == 9 || P == 11) ? 4 : 3;
 }
 
+// Even-odd body: F_y / F_z formed on the fly rather than staged at the orders
+// where that measured faster in the batch on GB300 (1.05x at p = 6, 1.11x at
+// p = 8; 0.96-0.97x at p = 10 and 11).
+template <int P>
+__host__ __device__ constexpr bool batch_eo_fly() {
+  return P == 6 || P == 8;
+}
+
 template <int P, int EO, int RK>
 __global__ void __launch_bounds__(kBatchThreadsMax, batch_min_blocks<P, EO>())
     batch_order_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
@@ -96,7 +104,7 @@ __global__ void __launch_bounds__(kBatchThreadsMax, batch_min_blocks<P, EO>())
           a.eo_sDf[d] = I.eo_sD[stage][d];
           a.eo_sLf[d] = I.eo_sL[stage][d];
         }
-        stage_eo_block<P, float, RK>(a, w.e_begin, w.e_count, smem);
+        stage_eo_block<P, float, RK, batch_eo_fly<P>()>(a, w.e_begin, w.e_count, smem);
       } else {
         stage_block<P, float, float, false, RK>(a, w.e_begin, w.e_count, smem);
       }
@@ -145,7 +153,7 @@ __global__ void init_blob_kernel(double* q, float* u, float* v, float* w, const 
 
 template <int P>
 size_t smem_for(int epb, int eo) {
-  return eo ? eo_block_smem<P, float>(epb) : stage_block_smem<P, float>(epb);
+  return eo ? eo_block_smem<P, float, batch_eo_fly<P>()>(epb) : stage_block_smem<P, float>(epb);
 }
 
 }  // namespace
@@ -217,8 +225,8 @@ int with_group(int p, int eo, F&& f) {
 void batch_default_shape(int p, int* threads, int* epb) {
   // index = order; measured with sdg_ensemble_tune, block sizes 128/256/512
   static const int kThreads[kBatchMaxOrder + 1] = {256, 128, 128, 128, 128, 256,
-                                                   512, 512, 512, 256, 256, 512};
-  static const int kEpb[kBatchMaxOrder + 1] = {1, 64, 16, 8, 4, 4, 8, 4, 2, 1, 1, 1};
+                                                   128, 512, 256, 256, 256, 512};
+  static const int kEpb[kBatchMaxOrder + 1] = {1, 64, 16, 8, 4, 4, 2, 4, 2, 1, 1, 1};
   const int i = (p >= 1 && p <= kBatchMaxOrder) ? p : 0;
   *threads = kThreads[i];
   *epb = kEpb[i];

@@ -75,8 +75,8 @@ struct EoCfg {
 };
 
 // Dynamic shared memory of one block with nloc elements: the three scaled
-// direction tables, then per element q, F_x (later the line-result sums), F_y,
-// F_z and the 6 Nfp face fluxes, then the neighbour indices.
+// direction tables, then per element the arrays below and the 6 Nfp face
+// fluxes, then the neighbour indices.
 // The FP64 body does not stage q: the face flux and the RK update read it
 // from global memory (L1 / L2 hits after phase 0), which saves shared memory
 // for a fourth resident block.
@@ -85,16 +85,20 @@ __host__ __device__ constexpr bool eo_stages_q() {
   return sizeof(CT) == 4;
 }
 
-// (The FP32 body keeps the line-result sums in their own array, since two
-// threads share a line and one may write before the other has read.)
 // The FP64 body keeps one array: the x lines' pair values, then the sums; the
 // y and z line threads form their lines' pair values from q and v / w in
-// cache.  That leaves room for four resident blocks.
-template <int P, typename CT>
+// cache.  That leaves room for four resident blocks.  The FP32 body keeps q
+// (FP32), F_x and the line-result sums (in their own array, since two threads
+// share a line and one may write before the other has read), and either
+// stages F_y and F_z as well or (FLY) has the y and z line threads form
+// F = q v / q w from the staged q and the velocity in cache: two arrays less,
+// which keeps more blocks resident at high orders, for two extra velocity
+// reads per line node.
+template <int P, typename CT, bool FLY = false>
 __host__ __device__ constexpr size_t eo_block_smem(int nloc) {
   using O = Ord<P>;
   constexpr int arrays =
-      sizeof(CT) == 8 ? 1 : (eo_stages_q<CT>() ? 4 : 3) + (eo_parts<CT>() > 1 ? 1 : 0);
+      sizeof(CT) == 8 ? 1 : (eo_stages_q<CT>() ? 2 : 1) + (FLY ? 0 : 2) + (eo_parts<CT>() > 1 ? 1 : 0);
   return sizeof(CT) * (size_t)(3 * EoShape<P>::TE + nloc * (arrays * O::NP + O::NFT)) +
          sizeof(int) * 6 * (size_t)nloc;
 }
@@ -113,16 +117,17 @@ __device__ __forceinline__ float abs_ct(float x) { return fabsf(x); }
 // PAIRED: F holds S(l) at l and Δ(l) at N-1-l (l < N/2) and, for odd N, F
 // at the middle, formed when the line was loaded; otherwise F holds the N
 // fluxes and the pair values are formed here.
-template <int P, int S, int PARTS, bool PAIRED, typename CT, typename Emit>
-__device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, CT gm, CT gp,
-                                        int part, Emit&& emit) {
+// Load(l) returns the line's value at node l (l < N).
+template <int P, int PARTS, bool PAIRED, typename CT, typename Load, typename Emit>
+__device__ __forceinline__ void eo_line_f(Load&& F, const CT* __restrict__ T, CT gm, CT gp,
+                                          int part, Emit&& emit) {
   using Sh = EoShape<P>;
   constexpr int N = Sh::N, H = Sh::H;
   constexpr int RPP = (H + PARTS - 1) / PARTS;
   CT s[H], d[H];
 #pragma unroll
   for (int l = 0; l < H; l++) {
-    const CT lo = F[l * S], hi = F[(N - 1 - l) * S];
+    const CT lo = F(l), hi = F(N - 1 - l);
     if constexpr (PAIRED) {
       s[l] = lo;
       d[l] = hi;
@@ -132,7 +137,7 @@ __device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, C
     }
   }
   CT fm = CT(0);
-  if constexpr (Sh::ODD != 0) fm = F[H * S];
+  if constexpr (Sh::ODD != 0) fm = F(H);
   const CT gs = gm + gp, gd = gm - gp;
   // rows unrolled up to p = 7 in FP32 and p = 4 in FP64; above that a rolled
   // loop keeps the 2H line values and the row sums within the register budget
@@ -163,6 +168,12 @@ __device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, C
   }
 }
 
+template <int P, int S, int PARTS, bool PAIRED, typename CT, typename Emit>
+__device__ __forceinline__ void eo_line(const CT* F, const CT* __restrict__ T, CT gm, CT gp,
+                                        int part, Emit&& emit) {
+  eo_line_f<P, PARTS, PAIRED, CT>([&](int l) { return F[l * S]; }, T, gm, gp, part, emit);
+}
+
 // Pair values of one line from q and the axis velocity in global memory (FP64
 // body): S(c) = F(c) + F(N-1-c) and Δ(c) = F(c) - F(N-1-c) with F = q u, as
 // P' = q' u' and fma(q, u, ±P') -- three operations a pair instead of four.
@@ -189,7 +200,7 @@ __device__ __forceinline__ void eo_pairs_f64(const double* __restrict__ q,
 // sums, scaled by eo_sDf / eo_sLf), with the increment widened by bits and
 // the RK combination in FP64.  Block size and nloc are runtime values, so the
 // batched persistent kernel can use the same body.
-template <int P, typename CT, int RKFIX = -1>
+template <int P, typename CT, int RKFIX = -1, bool FLY = false>
 __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb, int nloc,
                                                unsigned char* smem) {
   using O = Ord<P>;
@@ -202,11 +213,12 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   constexpr bool kSQ = eo_stages_q<CT>();
   CT* sq = sT + 3 * TE;      // q (FP32 body only)
   CT* sFx = sq + (kSQ ? nloc * NP : 0);  // F_x (FP64: x pair values), then the sums
-  CT* sFy = sFx + (kF64 ? 0 : nloc * NP);  // FP32 only
-  CT* sFz = sFy + (kF64 ? 0 : nloc * NP);  // FP32 only
+  constexpr bool kSYZ = !kF64 && !FLY;    // F_y, F_z staged (FP32 only)
+  CT* sFy = sFx + (kSYZ ? nloc * NP : 0);
+  CT* sFz = sFy + (kSYZ ? nloc * NP : 0);
   constexpr int PARTS = eo_parts<CT>();
   CT* sAcc = (PARTS > 1) ? sFz + nloc * NP : sFx;  // line-result sums
-  CT* sf = kF64 ? sFx + nloc * NP : sFz + nloc * NP * (PARTS > 1 ? 2 : 1);
+  CT* sf = sAcc + nloc * NP;
   int* snb = reinterpret_cast<int*>(sf + nloc * NFT);
 
   const double* __restrict__ qin = a.q_in;
@@ -260,8 +272,10 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
       const CT qq = to_ct<CT>(qin[g0 + t]);
       if constexpr (kSQ) sq[t] = qq;
       sFx[t] = qq * gu[g0 + t];
-      sFy[t] = qq * gv[g0 + t];
-      sFz[t] = qq * gw[g0 + t];
+      if constexpr (kSYZ) {
+        sFy[t] = qq * gv[g0 + t];
+        sFz[t] = qq * gw[g0 + t];
+      }
     }
   }
   __syncthreads();
@@ -317,9 +331,15 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
       eo_pairs_f64<P>(qin, gv, g0 + off, NQ, row);
       eo_line<P, 1, PARTS, true>(row, sT + TE, fl[0], fl[2 * NFP], part,
                                  [&](int m, CT v) { acc[m * NQ] += v; });
-    } else {
+    } else if constexpr (kSYZ) {
       eo_line<P, NQ, PARTS, false>(sFy + off, sT + TE, fl[0], fl[2 * NFP], part,
                                    [&](int m, CT v) { acc[m * NQ] += v; });
+    } else {
+      const CT* qr = sq + off;
+      const CT* vr = gv + g0 + off;
+      eo_line_f<P, PARTS, false, CT>([&](int l) { return qr[l * NQ] * vr[l * NQ]; }, sT + TE,
+                                     fl[0], fl[2 * NFP], part,
+                                     [&](int m, CT v) { acc[m * NQ] += v; });
     }
   }
   __syncthreads();
@@ -355,9 +375,14 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
         double row[NQ];
         eo_pairs_f64<P>(qin, gw, g0 + off, NQ2, row);
         eo_line<P, 1, PARTS, true>(row, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], part, emitz);
-      } else {
+      } else if constexpr (kSYZ) {
         eo_line<P, NQ2, PARTS, false>(sFz + off, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], part,
                                       emitz);
+      } else {
+        const CT* qr = sq + off;
+        const CT* wr = gw + g0 + off;
+        eo_line_f<P, PARTS, false, CT>([&](int l) { return qr[l * NQ2] * wr[l * NQ2]; },
+                                       sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], part, emitz);
       }
     }
   });
@@ -375,6 +400,14 @@ __host__ __device__ constexpr int eo_min_blocks() {
   return sizeof(CT) == 8 ? 4 : (P <= 12 ? 4 : 3);
 }
 
+// FP32 single-box kernel: F_y / F_z formed on the fly (FLY) at the orders
+// where that measured faster on GB300 (1.07-1.18x at p = 10, 13 and 15, even
+// at 12 and 14); staging them is faster below (up to 1.15x at p = 6).
+template <int P>
+__host__ __device__ constexpr bool eo_fly_single() {
+  return P == 10 || P >= 12;
+}
+
 template <int P, typename CT>
 __global__ void __launch_bounds__(EoCfg<P, CT>::THREADS, eo_min_blocks<P, CT>())
     stage_eo_kernel(const StageArgs a) {
@@ -384,12 +417,12 @@ __global__ void __launch_bounds__(EoCfg<P, CT>::THREADS, eo_min_blocks<P, CT>())
   const long long eend = a.elem_begin + a.elem_count;
   const int nloc = (int)((eend - eb) < EPB ? (eend - eb) : EPB);
   if (nloc <= 0) return;
-  stage_eo_block<P, CT>(a, eb, nloc, smem_raw);
+  stage_eo_block<P, CT, -1, eo_fly_single<P>()>(a, eb, nloc, smem_raw);
 }
 
 template <int P, typename CT>
 int launch_stage_eo_impl(const StageArgs& a, cudaStream_t st) {
-  constexpr size_t smem = eo_block_smem<P, CT>(EoCfg<P, CT>::EPB);
+  constexpr size_t smem = eo_block_smem<P, CT, eo_fly_single<P>()>(EoCfg<P, CT>::EPB);
   static bool attr_done = false;
   if (!attr_done) {
     SDG_CUDA_TRY(cudaFuncSetAttribute(stage_eo_kernel<P, CT>,
