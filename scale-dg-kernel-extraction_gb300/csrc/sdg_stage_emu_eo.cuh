@@ -4,9 +4,10 @@
 //
 // Per line of an axis d, with the line base F0 = q u_d at the line's node 0
 // and the differences G(l) = q u_d - F0 formed by one FP64 FMA (exact product
-// minus the base, rounded once), the pair values
-//     S(l) = G(l) + G(N-1-l),   Δ(l) = G(l) - G(N-1-l)      (l < N/2, FP64)
-// are split to double-float, and
+// minus the base, rounded once) and split to double-float, the pair values
+//     S(l) = G(l) + G(N-1-l),   Δ(l) = G(l) - G(N-1-l)      (l < N/2)
+// are double-float sums (TwoSum, no FP64 instruction: the differences are of
+// the size of the line's variation, so S and Δ keep 2^-48 of it), and
 //     e_i = Σ_l E(i,l) S(l) + R(i) F0 [+ D(i,mid) G(mid)] + B(i) gd,
 //     o_i = Σ_l O(i,l) Δ(l) + A(i) gs,
 //     out(i) = e_i + o_i,  out(N-1-i) = o_i - e_i,
@@ -56,7 +57,8 @@ constexpr size_t emu_eo_smem_bytes() {
 }
 
 // Pair values of one line from global memory: F0 = q u at the line's node 0,
-// G = q u - F0 by one FMA, S and Δ in FP64, split; written to row[0..N).
+// G = q u - F0 by one FMA, split, S and Δ in double-float; written to
+// row[0..N).
 template <int P>
 __device__ __forceinline__ void emu_eo_pairs(const double* __restrict__ q,
                                              const double* __restrict__ vel, long long g0,
@@ -67,9 +69,9 @@ __device__ __forceinline__ void emu_eo_pairs(const double* __restrict__ q,
 #pragma unroll
   for (int c = 0; c < H; c++) {
     const long long a = g0 + (long long)c * stride, b = g0 + (long long)(N - 1 - c) * stride;
-    const double G1 = fma(q[a], vel[a], -f0);
-    const double G2 = fma(q[b], vel[b], -f0);
-    const dfl S = df_split(G1 + G2), D = df_split(G1 - G2);
+    const dfl g1 = df_split(fma(q[a], vel[a], -f0));
+    const dfl g2 = df_split(fma(q[b], vel[b], -f0));
+    const dfl S = df_add(g1, g2), D = df_sub(g1, g2);
     row[c] = make_float2(S.hi, S.lo);
     row[N - 1 - c] = make_float2(D.hi, D.lo);
   }
@@ -230,7 +232,7 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS, emu_eo_min_blocks<P>())
     sg[t] = make_float2(gf.hi, gf.lo);
   }
   // phase 1b: x pair values per (line, c < ceil(N/2)): the differences
-  // G = q u - F0 by one FMA each, then S and Δ in FP64, split
+  // G = q u - F0 by one FMA each, split, then S and Δ in double-float
   for (int t = threadIdx.x; t < nloc * HR * NQ2; t += T) {
     const int le = t / (HR * NQ2);
     const int w = t - le * HR * NQ2;
@@ -244,8 +246,9 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS, emu_eo_min_blocks<P>())
     const double G1 = fma(qin[ge + n], gvel[ge + n], -f0);
     if (c < H) {
       const int n2 = line_node(d, r, NQ - 1 - c);
-      const double G2 = fma(qin[ge + n2], gvel[ge + n2], -f0);
-      const dfl S = df_split(G1 + G2), D = df_split(G1 - G2);
+      const dfl g1 = df_split(G1);
+      const dfl g2 = df_split(fma(qin[ge + n2], gvel[ge + n2], -f0));
+      const dfl S = df_add(g1, g2), D = df_sub(g1, g2);
       row[c] = make_float2(S.hi, S.lo);
       row[NQ - 1 - c] = make_float2(D.hi, D.lo);
     } else {
