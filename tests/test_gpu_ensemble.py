@@ -148,6 +148,20 @@ def test_explicit_shapes_and_graph_replay_compose():
         assert np.array_equal(ens.download(i), want)
 
 
+def test_many_one_element_members():
+    """600 single-element boxes of every order 1..11 (one element per work
+    item, 600 instance headers): a sample equals the standalone solver."""
+    members = [((1, 1, 1), 1 + i % 11) for i in range(600)]
+    ens, fields, dts, ops = build(members, seed0=600)
+    ens.tune()
+    ens.step(3)
+    for i in range(0, 600, 37):
+        dims, p = members[i]
+        opt = sdg.OPT_EVENODD if ens.config()["body"][p] == "evenodd" else sdg.OPT_GENERAL
+        want = standalone(dims, p, fields[i], dts[i], ops, 3, opt)
+        assert np.array_equal(ens.download(i), want), (i, p)
+
+
 def test_device_initial_condition_matches_host_recipe():
     dims, p = (3, 2, 2), 4
     ops = {p: operators(p)}

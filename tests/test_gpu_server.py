@@ -131,6 +131,38 @@ def test_admission_waits_for_memory_and_rejects_what_never_fits(ops):
     srv.close()
 
 
+def test_many_concurrent_submitters(ops):
+    """200 small requests from four submitting threads while earlier ones
+    run: every one completes, and a sample equals the same request alone."""
+    import threading
+    srv = sdg.Server(ops, max_active=64)
+    rs = [req((1 + i % 3, 2, 1 + i % 2), ORDERS[i % len(ORDERS)], 5 + i % 7, 100 + i)
+          for i in range(200)]
+    tickets = [None] * len(rs)
+
+    def submit(lo):
+        for i in range(lo, len(rs), 4):
+            tickets[i] = srv.submit(**rs[i], want_state=(i % 25 == 0))
+
+    th = [threading.Thread(target=submit, args=(k,)) for k in range(4)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    outs = {}
+    for i, tk in enumerate(tickets):
+        res, q = srv.wait(tk, timeout_s=600)
+        assert res["status"] == 0
+        if q is not None:
+            outs[i] = q
+    assert srv.stats()["completed"] == 200 and srv.stats()["fatal_status"] == 0
+    srv.close()
+    alone = sdg.Server(ops)
+    for i, q in outs.items():
+        assert np.array_equal(alone.wait(alone.submit(**rs[i], want_state=True))[1], q), i
+    alone.close()
+
+
 def test_wait_is_bounded(ops):
     srv = sdg.Server(ops)
     t = srv.submit(**req((6, 6, 6), 11, 400, 51))
