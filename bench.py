@@ -419,12 +419,15 @@ def bench_order_sweep(sdg, args):
     return out
 
 
-def bench_dropin(sdg, args, wl, fused_rate):
+def bench_dropin(sdg, args, wl, fused_rate, opt=None):
     """The reference-shaped per-stage path on the bench workload, all on device
     arrays: mesh arrays built on the device (sdg_mesh_setup_dev), then per step
     q0 = q and three times update_halo(q), advect3d_eq_cal_tend(...) and the RK
     stage, as main.f90:51-80 calls them.  Timed on the host around K steps
-    (queued asynchronously on one stream, launch cost included)."""
+    (queued asynchronously on one stream, launch cost included).  opt: the
+    tendency's type (OPT1, the reference's order, by default; EVENODD the
+    even-odd tendency kernel)."""
+    opt = sdg.OPT_OPT1 if opt is None else opt
     import ctypes as C
     p, ne = args.p, args.ne
     nq, np_ = p + 1, (p + 1) ** 3
@@ -459,7 +462,7 @@ def bench_dropin(sdg, args, wl, fused_rate):
             lib.sdg_update_halo_dev(q.ptr, hm.ptr, np_, ne3, nhn, None)
             lib.sdg_advect3d_eq_cal_tend_dev(dqdt.ptr, q.ptr, u.ptr, v.ptr, w.ptr, D.ptr, Dt.ptr,
                                              L.ptr, vm.ptr, vp.ptr, nf.ptr, es.ptr, fs.ptr, nq,
-                                             np_, ntf, ne3, nea, sdg.OPT_OPT1, flux.ptr, err.ptr,
+                                             np_, ntf, ne3, nea, opt, flux.ptr, err.ptr,
                                              None)
             lib.sdg_rk_stage_dev(q.ptr, q0.ptr, dqdt.ptr, np_, ne3, stage, dt, None)
 
@@ -478,9 +481,11 @@ def bench_dropin(sdg, args, wl, fused_rate):
     # streams: Escale 24 B per DOF, VMapM/VMapP/normal_fn/Fscale 40 B per face
     # node (6/Nq face nodes per DOF)
     bpd = BYTES_PER_DOF_UPDATE["fp64"] + 24.0 + 40.0 * 6.0 / nq
+    oname = {sdg.OPT_OPT1: "OPT1 order", sdg.OPT_GENERAL: "GENERAL order",
+             sdg.OPT_EVENODD: "even-odd tendency kernel"}[opt]
     return {"workload": f"same {ne}^3 p={p} box through the per-stage device entry points "
                         "(update_halo, advect3d_eq_cal_tend_dev with VMapM/VMapP gathers, "
-                        "rk_stage_dev, OPT1 order) as the reference's loop calls them",
+                        f"rk_stage_dev, {oname}) as the reference's loop calls them",
             "gdof_updates_per_s": rate, "ms_per_step": 1e3 * t / k, "steps": k,
             "launches_per_step": 13, "fused_over_dropin": fused_rate / rate,
             "bytes_per_dof_update_with_geometry": bpd,
@@ -711,6 +716,7 @@ def run_ours(args, ws, rank, local):
         line["fp64_emulated"] = other
     if ws == 1 and not args.no_dropin:
         line["dropin"] = bench_dropin(sdg, args, wl, value)
+        line["dropin_evenodd"] = bench_dropin(sdg, args, wl, value, sdg.OPT_EVENODD)
     if ws == 1 and not args.no_ensemble:
         line["ensemble"] = bench_ensemble(sdg, args)
     if ws == 1 and not args.no_serving:

@@ -100,9 +100,10 @@ int sdg_operator_generate(int p, double* x1D, double* D1D, double* D1D_tr,
 /* ---- drop-in for mod_dg_optr_kernel / mod_advect3d_eq ------------------ */
 
 /* dg_optr_kernel_setup (mod_dg_optr_kernel.f90:45-58): "GENERAL" or "OPT1"
- * (trailing blanks ignored, as trim() does).  Unlike the reference, an
- * unknown string returns SDG_ERR_BAD_OPTTYPE and leaves the setting as it
- * was. */
+ * (trailing blanks ignored, as trim() does), or "EVENODD" (no reference
+ * counterpart: cal_tend uses the even-odd line sums; the operator entry
+ * points use the GENERAL order).  Unlike the reference, an unknown string
+ * returns SDG_ERR_BAD_OPTTYPE and leaves the setting as it was. */
 int sdg_dg_optr_kernel_setup(const char* dgoptr_evaltype);
 /* The current default type (SDG_OPT_*), or 0 if never set. */
 int sdg_dg_optr_kernel_type(void);
@@ -125,7 +126,11 @@ int sdg_advect3d_eq_cal_tend(double* dqdt, const double* q, const double* u,
  * of NfpTot*Ne doubles for the element-boundary flux (the reference's
  * automatic array ebnd_flux, mod_advect3d_eq.f90:66); `err_flag` is a
  * caller-owned device int that the kernels set to 1 when a VMap index is out
- * of range (it is not cleared here). */
+ * of range, and with opt = SDG_OPT_EVENODD to 2 when D1D is not
+ * centro-antisymmetric, D1D_tr not its transpose or Lift_mat not separable
+ * and mirrored (it is not cleared here).  SDG_OPT_EVENODD honours the
+ * caller's per-node Escale and face fluxes; the host-pointer form returns
+ * SDG_ERR_INVALID_ARG for flag 2. */
 int sdg_advect3d_eq_cal_tend_dev(double* dqdt, const double* q,
                                  const double* u, const double* v,
                                  const double* w, const double* D1D,

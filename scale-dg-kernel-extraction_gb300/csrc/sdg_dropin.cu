@@ -40,8 +40,10 @@ static int dropin(int p, int what, int opt, const void* args, cudaStream_t st) {
   }
 }
 
+// GENERAL and OPT1 as the reference; EVENODD selects the even-odd tendency
+// kernel in cal_tend and the GENERAL order in the operator entry points.
 static int check_opt(int opt) {
-  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1)
+  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1 && opt != SDG_OPT_EVENODD)
     return fail(SDG_ERR_BAD_OPTTYPE,
                 "DGOptrKernel type not set (call sdg_dg_optr_kernel_setup) or "
                 "unknown (%d)", opt);
@@ -101,6 +103,10 @@ __global__ void flux_kernel(const TendArgs a, int NfpTot) {
     const double n1 = a.normal_fn[m], n2 = a.normal_fn[m + NT],
                  n3 = a.normal_fn[m + 2 * NT];
     const double qM = a.q[iM], qP = a.q[iP];
+    // all six velocity gathers are independent of the normals, so they are
+    // in flight together (a branch on the normal's axis that gathered one
+    // component per side measured 3 % slower: its gathers waited on the
+    // normal loads)
     const double VelM = a.u[iM] * n1 + a.v[iM] * n2 + a.w[iM] * n3;
     const double VelP = a.u[iP] * n1 + a.v[iP] * n2 + a.w[iP] * n3;
     const double alpha = 0.5 * fabs(VelP + VelM);
@@ -226,6 +232,9 @@ int sdg_advect3d_eq_cal_tend(double* dqdt, const double* q, const double* u,
   SDG_CUDA_TRY(cudaMemcpyAsync(&err, ar.at<void>(oR), sizeof(int), cudaMemcpyDeviceToHost, st));
   SDG_CUDA_TRY(cudaMemcpyAsync(dqdt, ar.at<void>(od), 8 * nO, cudaMemcpyDeviceToHost, st));
   SDG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (err == 2)
+    return fail(SDG_ERR_INVALID_ARG,
+                "D1D / D1D_tr / Lift_mat lack the even-odd symmetries; use GENERAL or OPT1");
   if (err) return fail(SDG_ERR_MESH, "a VMapM/VMapP entry is outside 1..Np*NeA");
   return SDG_OK;
 }

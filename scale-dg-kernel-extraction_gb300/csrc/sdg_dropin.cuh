@@ -6,12 +6,16 @@
 //                    thread per face node, VMap indices range-checked;
 //   dqdt_kernel      cal_dqdt (mod_advect3d_eq.f90:146-201), EPB elements
 //                    per block staged in shared memory;
+//   dqdt_eo_kernel   the same tendency with the even-odd line sums of the
+//                    fused stage (opt type SDG_OPT_EVENODD), honouring the
+//                    caller's per-node Escale and face fluxes;
 //   divlike_kernel   tensorprod_divlike_dirXYZ (mod_dg_optr_kernel.f90:62-136)
 //                    over a batch of elements;
 //   lift_kernel      tensorprod_Lift_hexahedral (mod_dg_optr_kernel.f90:139-190).
 #pragma once
 
 #include "sdg_stage.cuh"
+#include "sdg_stage_eo.cuh"
 
 namespace sdg {
 
@@ -89,6 +93,213 @@ __global__ void __launch_bounds__(DropCfg<P>::THREADS) dqdt_kernel(const TendArg
     a.dqdt[g] = -(((a.Escale[g] * dx + a.Escale[g + NpNe] * dy) +
                    a.Escale[g + 2 * NpNe] * dz) + lf);
   }
+}
+
+// ---- even-odd cal_dqdt --------------------------------------------------
+
+template <int P>
+struct DqdtEoCfg {
+  static constexpr int THREADS = 256;
+  static constexpr int EPB = (256 / Ord<P>::NQ2) > 0 ? 256 / Ord<P>::NQ2 : 1;
+};
+
+template <int P>
+constexpr size_t dqdt_eo_smem_bytes() {
+  return sizeof(double) * (size_t)(3 * EoShape<P>::TE + DqdtEoCfg<P>::EPB * Ord<P>::NP) +
+         2 * sizeof(unsigned long long);
+}
+
+// One line in pair form: s / d hold S(l) / Δ(l) (l < N/2), fm F(mid) for an
+// odd N; T the direction's unscaled tables; gm / gp the caller's face fluxes
+// of the line's - and + faces.  emit(m, dpart, lpart) receives, for position
+// m, the derivative sum (times Escale by the caller) and the lift sum apart.
+template <int P, typename Emit>
+__device__ __forceinline__ void eo_line_dl(const double* row, const double* __restrict__ T,
+                                           double gm, double gp, Emit&& emit) {
+  using Sh = EoShape<P>;
+  constexpr int N = Sh::N, H = Sh::H;
+  double s[H], d[H];
+#pragma unroll
+  for (int l = 0; l < H; l++) {
+    s[l] = row[l];
+    d[l] = row[N - 1 - l];
+  }
+  double fm = 0.0;
+  if constexpr (Sh::ODD != 0) fm = row[H];
+  const double gs = gm + gp, gd = gm - gp;
+  constexpr int kRowUnroll = (N <= 5) ? H : 1;
+#pragma unroll kRowUnroll
+  for (int i = 0; i < H; i++) {
+    double e = T[Sh::OFF_E + i * H] * s[0];
+#pragma unroll
+    for (int l = 1; l < H; l++) e = fma(T[Sh::OFF_E + i * H + l], s[l], e);
+    if constexpr (Sh::ODD != 0) e = fma(T[Sh::OFF_DM + i], fm, e);
+    double o = T[Sh::OFF_O + i * H] * d[0];
+#pragma unroll
+    for (int l = 1; l < H; l++) o = fma(T[Sh::OFF_O + i * H + l], d[l], o);
+    const double le = T[Sh::OFF_B + i] * gd, lo = T[Sh::OFF_A + i] * gs;
+    emit(i, e + o, lo + le);
+    emit(N - 1 - i, o - e, lo - le);
+  }
+  if constexpr (Sh::ODD != 0) {
+    double o = T[Sh::OFF_O + H * H] * d[0];
+#pragma unroll
+    for (int l = 1; l < H; l++) o = fma(T[Sh::OFF_O + H * H + l], d[l], o);
+    emit(H, o, T[Sh::OFF_A + H] * gs);
+  }
+}
+
+// cal_dqdt (mod_advect3d_eq.f90:146-201) with the even-odd factorisation:
+// per line the divergence sum D F is formed from the pair values and the two
+// faces' lift from the lift columns, dqdt = -(sum_d (Escale_d * D_d F_d +
+// lift_d)).  Every block builds the unscaled tables from D1D and Lift_mat
+// (the lift column of a face from its tangential node (0, 0)); block 0 checks
+// the symmetries the factorisation needs -- D1D centro-antisymmetric, D1D_tr
+// its transpose, each face's lift constant over the tangential nodes, the +
+// face's column the mirror of the - face's, all to 1e-13 of the largest entry
+// -- and sets *err = 2 when one fails.  The summation order is neither
+// GENERAL's nor OPT1's; results agree with both to rounding.
+template <int P>
+__global__ void __launch_bounds__(DqdtEoCfg<P>::THREADS, 4) dqdt_eo_kernel(const TendArgs a) {
+  using O = Ord<P>;
+  using Sh = EoShape<P>;
+  constexpr int NQ = O::NQ, NQ2 = O::NQ2, NP = O::NP, NFP = O::NFP, NFT = O::NFT,
+                EPB = DqdtEoCfg<P>::EPB, T = DqdtEoCfg<P>::THREADS, TE = Sh::TE, N = Sh::N,
+                H = Sh::H, HR = Sh::HR;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* sT = reinterpret_cast<double*>(smem_raw);  // [3][TE]
+  double* sA = sT + 3 * TE;                          // [EPB][NP]: x pairs, then sums
+  unsigned long long* smax = reinterpret_cast<unsigned long long*>(sA + EPB * NP);
+  const long long eb = (long long)blockIdx.x * EPB;
+  const int nloc = (int)min((long long)EPB, (long long)a.Ne - eb);
+  if (nloc <= 0) return;
+  const double* __restrict__ D = a.D;
+  const double* __restrict__ L = a.Lift;
+  auto Dv = [&](int i, int l) { return D[i + l * N]; };  // D1D(i,l), column-major
+  auto Ds = [&](int i, int l) { return 0.5 * (Dv(i, l) - Dv(N - 1 - i, N - 1 - l)); };
+  // lift of face f at normal index m (tangential indices 0, 0) on axis ax
+  auto node = [](int ax, int m, int t1, int t2) {
+    return (ax == 0) ? m + NQ * t1 + NQ2 * t2 : (ax == 1) ? t1 + NQ * m + NQ2 * t2
+                                                           : t1 + NQ * t2 + NQ2 * m;
+  };
+  auto col = [&](int ax, int side, int m) {
+    const int f = (ax == 0) ? (side ? 1 : 3) : (ax == 1) ? (side ? 2 : 0) : (side ? 5 : 4);
+    return L[node(ax, m, 0, 0) + (long long)f * NP];
+  };
+  auto lam = [&](int ax, int m) { return 0.5 * (col(ax, 0, m) + col(ax, 1, N - 1 - m)); };
+  for (int t = threadIdx.x; t < 3 * TE; t += T) {
+    const int ax = t / TE, w = t - ax * TE;
+    double v;
+    if (w < Sh::OFF_O) {
+      const int i = w / H, l = w - i * H;
+      v = 0.5 * (Ds(i, l) + Ds(i, N - 1 - l));
+    } else if (w < Sh::OFF_DM) {
+      const int i = (w - Sh::OFF_O) / H, l = (w - Sh::OFF_O) - i * H;
+      v = 0.5 * (Ds(i, l) - Ds(i, N - 1 - l));
+    } else if (w < Sh::OFF_A) {
+      v = Ds(w - Sh::OFF_DM, H);
+    } else if (w < Sh::OFF_B) {
+      const int i = w - Sh::OFF_A;
+      v = 0.5 * (lam(ax, i) + lam(ax, N - 1 - i));
+    } else {
+      const int i = w - Sh::OFF_B;
+      v = 0.5 * (lam(ax, i) - lam(ax, N - 1 - i));
+    }
+    sT[t] = v;
+  }
+  if (blockIdx.x == 0) {
+    // the largest |D| and |Lift| (non-negative doubles order like their bits)
+    if (threadIdx.x == 0) smax[0] = smax[1] = 0ull;
+    __syncthreads();
+    unsigned long long mD = 0, mL = 0;
+    for (int t = threadIdx.x; t < NQ2; t += T) mD = max(mD, (unsigned long long)__double_as_longlong(fabs(D[t])));
+    for (int t = threadIdx.x; t < 6 * NP; t += T) mL = max(mL, (unsigned long long)__double_as_longlong(fabs(L[t])));
+    atomicMax(&smax[0], mD);
+    atomicMax(&smax[1], mL);
+    __syncthreads();
+    const double tD = 1e-13 * __longlong_as_double((long long)smax[0]);
+    const double tL = 1e-13 * __longlong_as_double((long long)smax[1]);
+    bool bad = false;
+    for (int t = threadIdx.x; t < NQ2; t += T) {
+      const int i = t % N, l = t / N;
+      bad |= fabs(Dv(i, l) + Dv(N - 1 - i, N - 1 - l)) > tD;
+      bad |= fabs(a.Dt[l + i * N] - Dv(i, l)) > tD;
+    }
+    for (int t = threadIdx.x; t < 6 * NP; t += T) {
+      const int f = t / NP, n = t - f * NP;
+      const int ax = (f == 1 || f == 3) ? 0 : (f == 0 || f == 2) ? 1 : 2;
+      const int side = (f == 1 || f == 2 || f == 5) ? 1 : 0;
+      const int c[3] = {n % NQ, (n / NQ) % NQ, n / NQ2};
+      bad |= fabs(L[t] - col(ax, side, c[ax])) > tL;
+      if (n < N && ax == 0 && side == 0)  // mirror, once per axis below
+        for (int x = 0; x < 3; x++) bad |= fabs(col(x, 0, n) - col(x, 1, N - 1 - n)) > tL;
+    }
+    if (bad) atomicExch(a.err, 2);
+  }
+  const long long g0 = eb * NP;
+  const double* __restrict__ q = a.q;
+  // x pair values: one task per (element, x line, c < ceil(N/2))
+  for (int t = threadIdx.x; t < nloc * NQ2 * HR; t += T) {
+    const int le = t / (NQ2 * HR), w = t - le * NQ2 * HR;
+    const int r = w / HR, c = w - r * HR;
+    const long long g = g0 + (long long)le * NP + (long long)r * NQ;
+    double* row = sA + le * NP + r * NQ;
+    if (c < H) {
+      const double q1 = q[g + c], u1 = a.u[g + c];
+      const double p2 = q[g + NQ - 1 - c] * a.u[g + NQ - 1 - c];
+      row[c] = fma(q1, u1, p2);
+      row[NQ - 1 - c] = fma(q1, u1, -p2);
+    } else {
+      row[c] = q[g + c] * a.u[g + c];
+    }
+  }
+  __syncthreads();
+  const long long NpNe = (long long)NP * a.Ne;
+  const int r = threadIdx.x % NQ2, le = threadIdx.x / NQ2;
+  const bool has_line = threadIdx.x < nloc * NQ2;
+  const double* fl = a.flux + (eb + le) * NFT + r;
+  // x lines: faces -x (3) and +x (1); results over the pair values
+  if (has_line) {
+    double* row = sA + le * NP + r * NQ;
+    const long long g = g0 + (long long)le * NP + (long long)r * NQ;
+    eo_line_dl<P>(row, sT, fl[3 * NFP], fl[1 * NFP], [&](int m, double vd, double vl) {
+      row[m] = fma(a.Escale[g + m], vd, vl);
+    });
+  }
+  __syncthreads();
+  // y lines: faces -y (0) and +y (2); added into the sums
+  if (has_line) {
+    const int off = le * NP + (r % NQ) + (r / NQ) * NQ2;
+    double row[NQ];
+    eo_pairs_f64<P>(q, a.v, g0 + off, NQ, row);
+    eo_line_dl<P>(row, sT + TE, fl[0], fl[2 * NFP], [&](int m, double vd, double vl) {
+      const int n = off + m * NQ;
+      sA[n] += fma(a.Escale[g0 + n + NpNe], vd, vl);
+    });
+  }
+  __syncthreads();
+  // z lines: faces -z (4) and +z (5); finish the node
+  if (has_line) {
+    const int off = le * NP + r;
+    double row[NQ];
+    eo_pairs_f64<P>(q, a.w, g0 + off, NQ2, row);
+    eo_line_dl<P>(row, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP], [&](int m, double vd, double vl) {
+      const int n = off + m * NQ2;
+      a.dqdt[g0 + n] = -(sA[n] + fma(a.Escale[g0 + n + 2 * NpNe], vd, vl));
+    });
+  }
+}
+
+template <int P>
+int launch_dqdt_eo_impl(const TendArgs& a, cudaStream_t st) {
+  constexpr size_t smem = dqdt_eo_smem_bytes<P>();
+  SDG_CUDA_TRY(cudaFuncSetAttribute(dqdt_eo_kernel<P>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long long nblk = ((long long)a.Ne + DqdtEoCfg<P>::EPB - 1) / DqdtEoCfg<P>::EPB;
+  if (nblk == 0) return SDG_OK;
+  dqdt_eo_kernel<P><<<(unsigned)nblk, DqdtEoCfg<P>::THREADS, smem, st>>>(a);
+  SDG_CUDA_TRY(cudaGetLastError());
+  return SDG_OK;
 }
 
 struct DivArgs {
@@ -260,6 +471,7 @@ int dropin_order(int what, int opt, const void* args, cudaStream_t st) {
   switch (what) {
     case 0: {
       const TendArgs& a = *static_cast<const TendArgs*>(args);
+      if (opt == SDG_OPT_EVENODD) return launch_dqdt_eo_impl<P>(a, st);
       return split ? launch_dqdt_impl<P, kCanSplit>(a, st) : launch_dqdt_impl<P, false>(a, st);
     }
     case 1: {

@@ -437,6 +437,7 @@ int sdg_dg_optr_kernel_setup(const char* t) {
   while (!s.empty() && s.back() == ' ') s.pop_back();  // trim()
   if (s == "GENERAL") g_opttype = SDG_OPT_GENERAL;
   else if (s == "OPT1") g_opttype = SDG_OPT_OPT1;
+  else if (s == "EVENODD") g_opttype = SDG_OPT_EVENODD;
   else return fail(SDG_ERR_BAD_OPTTYPE, "Unsupported dgoptr_evaltype: %s", t);
   return SDG_OK;
 }

@@ -87,7 +87,7 @@ extern "C" int sdg_advect3d_eq_cal_tend_noalloc(
     const double* D1D, const double* D1D_tr, const double* Lift_mat, const int* VMapM,
     const int* VMapP, const double* normal_fn, const double* Escale, const double* Fscale,
     int Nq, int Np, int NfpTot, int Ne, int NeA, int opt, void* stream) {
-  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1)
+  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1 && opt != SDG_OPT_EVENODD)
     return fail(SDG_ERR_BAD_OPTTYPE, "unknown DGOptrKernel type %d", opt);
   if (Nq - 1 < 1 || Nq - 1 > kMaxOrder)
     return fail(SDG_ERR_UNSUPPORTED_ORDER, "PolyOrder %d outside 1..15", Nq - 1);
@@ -117,6 +117,9 @@ extern "C" int sdg_advect3d_eq_cal_tend_noalloc(
   int h_err = 0;
   SDG_CUDA_TRY(cudaMemcpyAsync(&h_err, sc.err, sizeof(int), cudaMemcpyDeviceToHost, st));
   SDG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (h_err == 2)
+    return fail(SDG_ERR_INVALID_ARG,
+                "D1D / D1D_tr / Lift_mat lack the even-odd symmetries; use GENERAL or OPT1");
   if (h_err) return fail(SDG_ERR_MESH, "a VMapM/VMapP entry is outside 1..Np*NeA");
   return SDG_OK;
 }

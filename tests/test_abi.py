@@ -64,6 +64,9 @@ def test_dg_optr_kernel_setup_accepts_reference_strings():
         sdg.dg_optr_kernel_setup("OPT2")
     assert e.value.status == sdg.ERR_BAD_OPTTYPE
     assert sdg.dg_optr_kernel_type() == sdg.OPT_OPT1  # unchanged by the failure
+    sdg.dg_optr_kernel_setup("EVENODD ")  # the even-odd extension
+    assert sdg.dg_optr_kernel_type() == sdg.OPT_EVENODD
+    sdg.dg_optr_kernel_setup("OPT1")
 
 
 def test_operator_generate_rejects_bad_order():

@@ -182,6 +182,99 @@ def test_dropin_cal_tend_matches_oracle(p, opt):
 
 
 @pytest.mark.parametrize("p", range(1, 16))
+def test_dropin_evenodd_cal_tend_matches_oracle(p):
+    """The even-odd tendency kernel behind the reference's cal_tend signature
+    (VMap gathers, the caller's flux, per-node Escale)."""
+    c = Case(*mesh_dims(p), p, ic="blob")
+    m = c.mesh
+    sdg.dg_optr_kernel_setup("EVENODD")
+    dqdt = np.full(m.Np * m.NeA, 7.0)
+    sdg.advect3d_eq_cal_tend(dqdt, c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, m.VMapM, m.VMapP,
+                             m.normal_fn, m.Escale, m.Fscale, m.Nq, m.Np, m.NfpTot, m.Ne, m.NeA)
+    sdg.dg_optr_kernel_setup("OPT1")
+    assert rel_l2(dqdt[: c.nown], c.oracle_tend(O.OPT1)) <= TOL_TEND
+    assert np.all(dqdt[c.nown:] == 7.0)
+
+
+@pytest.mark.parametrize("p", [2, 7, 10])
+def test_dropin_evenodd_honours_per_node_escale(p):
+    """Escale that varies node by node (not a constant per element and axis):
+    the even-odd kernel applies it after the line sums, like the reference."""
+    import copy
+    c = Case(*mesh_dims(p), p, ic="blob")
+    m = copy.copy(c.mesh)
+    rng = np.random.default_rng(900 + p)
+    m.Escale = c.mesh.Escale * (1.0 + 0.3 * rng.random(c.mesh.Escale.size))
+    sdg.dg_optr_kernel_setup("EVENODD")
+    dqdt = np.zeros(m.Np * m.NeA)
+    sdg.advect3d_eq_cal_tend(dqdt, c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, m.VMapM, m.VMapP,
+                             m.normal_fn, m.Escale, m.Fscale, m.Nq, m.Np, m.NfpTot, m.Ne, m.NeA)
+    sdg.dg_optr_kernel_setup("OPT1")
+    ref = O.cal_tend(m, c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, O.OPT1)[: c.nown]
+    assert rel_l2(dqdt[: c.nown], ref) <= TOL_TEND
+
+
+@pytest.mark.parametrize("opt", ["OPT1", "EVENODD"])
+def test_dropin_flux_with_oblique_normals(opt):
+    """Normals off the axes (the general u.n branch of the face flux) and
+    axis-aligned ones mixed in one mesh."""
+    import copy
+    c = Case(3, 2, 2, 4, ic="blob")
+    m = copy.copy(c.mesh)
+    nt = m.NfpTot * m.Ne
+    nf = c.mesh.normal_fn.copy().reshape(3, nt)
+    rng = np.random.default_rng(77)
+    pick = rng.random(nt) < 0.5
+    nf[:, pick] += 0.2 * rng.standard_normal((3, int(pick.sum())))
+    m.normal_fn = nf.reshape(-1)
+    sdg.dg_optr_kernel_setup(opt)
+    dqdt = np.zeros(m.Np * m.NeA)
+    sdg.advect3d_eq_cal_tend(dqdt, c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, m.VMapM, m.VMapP,
+                             m.normal_fn, m.Escale, m.Fscale, m.Nq, m.Np, m.NfpTot, m.Ne, m.NeA)
+    sdg.dg_optr_kernel_setup("OPT1")
+    ref = O.cal_tend(m, c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, O.OPT1)[: c.nown]
+    assert rel_l2(dqdt[: c.nown], ref) <= TOL_TEND
+
+
+def test_dropin_evenodd_refuses_operators_without_the_symmetry():
+    c = Case(2, 2, 2, 5, ic="blob")
+    m = c.mesh
+    args = (c.q, c.u, c.v, c.w)
+    geo = (m.VMapM, m.VMapP, m.normal_fn, m.Escale, m.Fscale, m.Nq, m.Np, m.NfpTot, m.Ne, m.NeA)
+    sdg.dg_optr_kernel_setup("EVENODD")
+    try:
+        badD = c.D.copy()
+        badD[3] *= 1.0 + 1e-9
+        with pytest.raises(sdg.SdgError) as e:
+            sdg.advect3d_eq_cal_tend(np.zeros(m.Np * m.NeA), *args, badD, badD.reshape(
+                m.Nq, m.Nq).T.copy().reshape(-1), c.Lift, *geo)
+        assert e.value.status == sdg.ERR_INVALID_ARG
+        badDt = c.Dt.copy()
+        badDt[5] += 1e-6
+        with pytest.raises(sdg.SdgError) as e:
+            sdg.advect3d_eq_cal_tend(np.zeros(m.Np * m.NeA), *args, c.D, badDt, c.Lift, *geo)
+        assert e.value.status == sdg.ERR_INVALID_ARG
+        badL = c.Lift.copy()
+        badL[m.Np + 9] *= 1.0 + 1e-9
+        with pytest.raises(sdg.SdgError) as e:
+            sdg.advect3d_eq_cal_tend(np.zeros(m.Np * m.NeA), *args, c.D, c.Dt, badL, *geo)
+        assert e.value.status == sdg.ERR_INVALID_ARG
+        # the device form reports the same through its flag (2)
+        arrs = [sdg.DeviceArray(a) for a in (c.q, c.u, c.v, c.w, c.D, c.Dt, badL, m.VMapM,
+                                             m.VMapP, m.normal_fn, m.Escale, m.Fscale)]
+        out = sdg.DeviceArray(n=m.Np * m.NeA)
+        flux = sdg.DeviceArray(n=m.NfpTot * m.Ne)
+        err = sdg.DeviceArray(np.zeros(1, dtype=np.int32))
+        assert sdg.lib.sdg_advect3d_eq_cal_tend_dev(out.ptr, *[a.ptr for a in arrs], m.Nq, m.Np,
+                                                    m.NfpTot, m.Ne, m.NeA, sdg.OPT_EVENODD,
+                                                    flux.ptr, err.ptr, None) == 0
+        sdg.synchronize()
+        assert err.numpy()[0] == 2
+    finally:
+        sdg.dg_optr_kernel_setup("OPT1")
+
+
+@pytest.mark.parametrize("p", range(1, 16))
 def test_gradlike_matches_oracle(p):
     x, D, Dt, L = operators(p)
     Nq, Np = p + 1, (p + 1) ** 3
@@ -239,7 +332,7 @@ def test_divlike_var5_matches_oracle(p):
         assert np.array_equal(dev[d].numpy(), got[d])
 
 
-@pytest.mark.parametrize("opt", ["OPT1", "GENERAL"])
+@pytest.mark.parametrize("opt", ["OPT1", "GENERAL", "EVENODD"])
 def test_dropin_single_element_box(opt):
     c = Case(1, 1, 1, 9, ic="blob")
     m = c.mesh
@@ -247,6 +340,7 @@ def test_dropin_single_element_box(opt):
     dqdt = np.zeros(m.Np * m.NeA)
     sdg.advect3d_eq_cal_tend(dqdt, c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, m.VMapM, m.VMapP,
                              m.normal_fn, m.Escale, m.Fscale, m.Nq, m.Np, m.NfpTot, m.Ne, m.NeA)
+    sdg.dg_optr_kernel_setup("OPT1")
     ref = c.oracle_tend(O.OPT1 if opt == "OPT1" else O.GENERAL)
     assert rel_l2(dqdt[: c.nown], ref) <= TOL_TEND
 

@@ -30,13 +30,13 @@ def _device_inputs(c: Case, vmapm=None):
                                          m.normal_fn, m.Escale, m.Fscale)]
 
 
-def _with_caller_scratch(c: Case, ins):
+def _with_caller_scratch(c: Case, ins, opt=sdg.OPT_OPT1):
     m = c.mesh
     out = sdg.DeviceArray(np.zeros(m.Np * m.NeA))
     flux = sdg.DeviceArray(n=m.NfpTot * m.Ne)
     err = sdg.DeviceArray(np.zeros(1, dtype=np.int32))
     st = sdg.lib.sdg_advect3d_eq_cal_tend_dev(out.ptr, *[a.ptr for a in ins], m.Nq, m.Np,
-                                              m.NfpTot, m.Ne, m.NeA, sdg.OPT_OPT1, flux.ptr,
+                                              m.NfpTot, m.Ne, m.NeA, opt, flux.ptr,
                                               err.ptr, None)
     assert st == 0
     sdg.synchronize()
@@ -44,11 +44,11 @@ def _with_caller_scratch(c: Case, ins):
     return out.numpy()[: c.nown]
 
 
-def _without_alloc(c: Case, ins):
+def _without_alloc(c: Case, ins, opt=sdg.OPT_OPT1):
     m = c.mesh
     out = sdg.DeviceArray(np.zeros(m.Np * m.NeA))
     st = _noalloc()(out.ptr, *[a.ptr for a in ins], m.Nq, m.Np, m.NfpTot, m.Ne, m.NeA,
-                    sdg.OPT_OPT1, None)
+                    opt, None)
     return st, out.numpy()[: c.nown]
 
 
@@ -83,3 +83,12 @@ def test_noalloc_rejects_sizes_beyond_its_array():
     st = _noalloc()(*([d.ptr] * 13), Nq, Nq ** 3, 6 * Nq * Nq, Ne, Ne, sdg.OPT_OPT1, None)
     assert st == sdg.ERR_INVALID_ARG
     assert b"at most" in sdg.lib.sdg_last_error()
+
+
+def test_noalloc_evenodd_matches_dev_entry_point():
+    c = Case(3, 2, 4, 6, ic="blob")
+    ins = _device_inputs(c)
+    st, got = _without_alloc(c, ins, sdg.OPT_EVENODD)
+    assert st == 0
+    assert np.array_equal(got, _with_caller_scratch(c, ins, sdg.OPT_EVENODD))
+    assert rel_l2(got, c.oracle_tend()) <= TOL_TEND
