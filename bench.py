@@ -753,7 +753,7 @@ def main() -> int:
                     help="summation order of the FP64 stage: the reference's GENERAL or "
                          "OPT1 order, or the even-odd factorised body")
     ap.add_argument("--seed", type=int, default=20261203)
-    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
