@@ -326,7 +326,7 @@ def bench_ensemble(sdg, args):
     t0 = time.perf_counter()
     ens = sdg.Ensemble([m["dims"] for m in members], [m["p"] for m in members],
                        [m["dt"] for m in members], ops)
-    if args.batch_opt != "evenodd":
+    if args.batch_opt != "auto":
         ens.set_opt(OPTS[args.batch_opt])
     ens.set_parallel_groups(args.parallel_groups)
     for i, m in enumerate(members):
@@ -515,7 +515,8 @@ def bench_serving(sdg, args, rate=None, plain_cache=None):
         t += -math.log(1.0 - rng.uniform()) / (rate or args.serve_rate)
         arrivals.append(t)
     srv = sdg.Server(ops, hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)),
-                     opt=OPTS[args.batch_opt], parallel_groups=args.parallel_groups)
+                     opt=0 if args.batch_opt == "auto" else OPTS[args.batch_opt],
+                     parallel_groups=args.parallel_groups)
     # warm the batched kernel and the pool
     srv.wait(srv.submit(**reqs[0]))
     srv.reset_stats()
@@ -762,8 +763,10 @@ def main() -> int:
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-dropin", action="store_true",
                     help="skip the per-stage drop-in path measurement")
-    ap.add_argument("--batch-opt", choices=["general", "evenodd"], default="evenodd",
-                    help="stage body of the batched kernel (ensemble and serving)")
+    ap.add_argument("--batch-opt", choices=["auto", "general", "evenodd"], default="auto",
+                    help="stage body of the batched kernels (ensemble and serving): auto = "
+                         "chosen per order (the ensemble's tuner, the server's measured "
+                         "defaults), else fixed for every order")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--sweep-steps", type=int, default=100)
     ap.add_argument("--no-serving", action="store_true")

@@ -76,6 +76,9 @@ struct BatchGroup {
 // autotuner's choices for the even-odd body on four boxes of about 3.5M DOF
 // of each order, on GB300.
 void batch_default_shape(int p, int* threads, int* epb);
+// Default stage body of order p (1: even-odd, 0: node body): the faster one
+// in the batched kernels on GB300 (the node body at p = 2 only).
+int batch_default_eo(int p);
 
 // Sets the group kernel's shared-memory limit and its grid from occupancy.
 int batch_group_setup(BatchGroup& g);

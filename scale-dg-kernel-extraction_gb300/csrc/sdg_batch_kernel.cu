@@ -232,6 +232,8 @@ void batch_default_shape(int p, int* threads, int* epb) {
   *epb = kEpb[i];
 }
 
+int batch_default_eo(int p) { return p == 2 ? 0 : 1; }
+
 int batch_group_setup(BatchGroup& g) {
   const int threads = g.threads;
   int dev = 0, nsm = 0;

@@ -108,13 +108,14 @@ int admit(sdg_server* s, Req* q) {
   I.u = vel;
   I.v = vel + nd;
   I.w = vel + 2 * nd;
+  I.p = q->r.p;
   I.D = s->d_ops[q->r.p][0];
   I.Lift = s->d_ops[q->r.p][1];
   I.eo_tab = s->d_ops[q->r.p][2];
-  I.eo = (I.eo_tab != nullptr) ? 1 : 0;
+  // opt 0: the measured default body of the order; EVENODD: even-odd everywhere
+  I.eo = (I.eo_tab != nullptr && (s->cfg.opt != 0 || batch_default_eo(I.p))) ? 1 : 0;
   I.dt = q->r.dt;
   batch_stage_factors(I);
-  I.p = q->r.p;
   I.cur = 0;
   I.active = 1;
   SDG_TRY(batch_init_blob(I, s->d_x1D[q->r.p], q->r.centre, q->r.sigma, q->r.velocity,

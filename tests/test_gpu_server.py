@@ -39,11 +39,13 @@ def mixed_ops(ops):
     return out
 
 
-@pytest.mark.parametrize("body", ["evenodd", "node", "mixed"])
+@pytest.mark.parametrize("body", ["default", "evenodd", "node", "mixed"])
 def test_result_is_the_same_alone_and_in_the_mix(ops, body):
     target = req((3, 4, 2), 5, 40, 11)
     if body == "node":
         srv = sdg.Server(ops, opt=sdg.OPT_GENERAL)
+    elif body == "evenodd":
+        srv = sdg.Server(ops, opt=sdg.OPT_EVENODD)
     elif body == "mixed":
         srv = sdg.Server(mixed_ops(ops))
     else:
@@ -85,6 +87,18 @@ def test_launch_shape_does_not_change_results(ops):
     for other in outs[1:]:
         for a, b in zip(outs[0], other):
             assert np.array_equal(a, b)
+
+
+def test_default_body_is_the_node_body_at_p2_and_even_odd_above(ops):
+    rs = {2: req((3, 2, 2), 2, 9, 61), 5: req((2, 3, 2), 5, 9, 62)}
+    got = {}
+    for name, opt in (("default", 0), ("node", sdg.OPT_GENERAL), ("evenodd", sdg.OPT_EVENODD)):
+        srv = sdg.Server(ops, opt=opt)
+        got[name] = {p: srv.wait(srv.submit(**r, want_state=True))[1] for p, r in rs.items()}
+        srv.close()
+    assert np.array_equal(got["default"][2], got["node"][2])
+    assert np.array_equal(got["default"][5], got["evenodd"][5])
+    assert not np.array_equal(got["node"][5], got["evenodd"][5])
 
 
 def test_bad_server_block_size_is_rejected(ops):
