@@ -254,27 +254,32 @@ void worker_loop(sdg_server* s) {
       s->cv_done.notify_all();
       continue;
     }
-    std::vector<Req*> still;
-    bool any_done = false;
+    std::vector<Req*> still, done;
     for (Req* q : s->active) {
       q->steps_done += k;
-      if (q->steps_done >= q->r.nstep) {
-        int fst = SDG_OK;
-        if (q->out) {
-          const long long nd = request_dofs(q->r);
-          cudaError_t ce = cudaMemcpyAsync(q->out, q->inst.q[q->steps_done % 3], 8 * nd,
-                                           cudaMemcpyDeviceToHost, s->stream);
-          if (ce == cudaSuccess) ce = cudaStreamSynchronize(s->stream);
-          if (ce != cudaSuccess) fst = cuda_fail(ce, "result copy", __FILE__, __LINE__);
-        }
-        finish(s, q, fst);
-        s->completed++;
-        s->latencies.push_back(std::chrono::duration<double>(q->t_done - q->t_submit).count());
-        s->t_last_done = q->t_done;
-        any_done = true;
-      } else {
-        still.push_back(q);
-      }
+      (q->steps_done >= q->r.nstep ? done : still).push_back(q);
+    }
+    const bool any_done = !done.empty();
+    // result copies run without the lock, so that submitters and waiters are
+    // not held up by them; only this thread touches a request's buffers
+    std::vector<int> fst(done.size(), SDG_OK);
+    lk.unlock();
+    for (size_t i = 0; i < done.size(); i++) {
+      Req* q = done[i];
+      if (!q->out) continue;
+      const long long nd = request_dofs(q->r);
+      cudaError_t ce = cudaMemcpyAsync(q->out, q->inst.q[q->steps_done % 3], 8 * nd,
+                                       cudaMemcpyDeviceToHost, s->stream);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(s->stream);
+      if (ce != cudaSuccess) fst[i] = cuda_fail(ce, "result copy", __FILE__, __LINE__);
+    }
+    lk.lock();
+    for (size_t i = 0; i < done.size(); i++) {
+      Req* q = done[i];
+      finish(s, q, fst[i]);
+      s->completed++;
+      s->latencies.push_back(std::chrono::duration<double>(q->t_done - q->t_submit).count());
+      s->t_last_done = q->t_done;
     }
     if (any_done) {
       s->active.swap(still);
