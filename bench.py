@@ -172,14 +172,15 @@ class OracleBox:
         return steps, time.perf_counter() - t0
 
 
-def load_traffic(key: str):
+def load_traffic(key: str, field: str = "bytes_per_launch"):
+    """A figure of one kernel's ncu capture (profiles/dram_traffic.json)."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         d = json.load(f)
     v = d.get(key)
-    return float(v["bytes_per_launch"]) if isinstance(v, dict) else None
+    return float(v[field]) if isinstance(v, dict) and field in v else None
 
 
 def run_reference(args, ws, rank):
@@ -291,6 +292,10 @@ def roofline(precision, p, ne, ndof, t, steps, peaks, opt="opt1"):
                      if opt == "evenodd" else "algorithmic flops")}
         if precision == "fp64":
             roof["binding_roof"] = "fp64_pipe" if roof["compute"]["frac"] > roof["frac"] else "hbm"
+        busy = load_traffic(tkey, "fp64_pipe_active")
+        if busy is not None:
+            # sm__pipe_fp64_cycles_active of the same kernel's ncu capture
+            roof["compute"]["fp64_pipe_active_ncu"] = busy
     return roof
 
 
