@@ -430,10 +430,10 @@ typedef struct {
                                order (0: the default of each order) */
   int epb_by_order[16];     /* elements per block by order (0: default) */
   int opt;                  /* stage body: 0 = the measured faster body per order
-                               (even-odd where the operators allow it, except
-                               the node body at p = 2); SDG_OPT_EVENODD =
-                               even-odd at every order; SDG_OPT_GENERAL /
-                               SDG_OPT_OPT1 = node body (running sums) */
+                               (currently even-odd at every order, where the
+                               operators allow it); SDG_OPT_EVENODD = even-odd;
+                               SDG_OPT_GENERAL / SDG_OPT_OPT1 = node body
+                               (running sums) */
   int threads_by_order[16]; /* block size by order (0: `threads`, else the
                                default of the order) */
   int parallel_groups;      /* 0: the order groups of a step run one after the

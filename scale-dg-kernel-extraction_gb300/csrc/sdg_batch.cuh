@@ -77,7 +77,9 @@ struct BatchGroup {
 // of each order, on GB300.
 void batch_default_shape(int p, int* threads, int* epb);
 // Default stage body of order p (1: even-odd, 0: node body): the faster one
-// in the batched kernels on GB300 (the node body at p = 2 only).
+// in the batched kernels on GB300, which is the even-odd body at every order
+// (at p = 2 since its lines take one thread each: 59.7 against 53.3
+// GDOF-updates/s for the node body).
 int batch_default_eo(int p);
 
 // Sets the group kernel's shared-memory limit and its grid from occupancy.

@@ -232,7 +232,7 @@ void batch_default_shape(int p, int* threads, int* epb) {
   *epb = kEpb[i];
 }
 
-int batch_default_eo(int p) { return p == 2 ? 0 : 1; }
+int batch_default_eo(int p) { return p >= 1 ? 1 : 0; }
 
 int batch_group_setup(BatchGroup& g) {
   const int threads = g.threads;

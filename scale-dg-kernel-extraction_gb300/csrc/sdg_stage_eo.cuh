@@ -62,15 +62,16 @@ struct EoShape {
 // Threads per line in the line phases: the FP32 body splits a line's output
 // pairs between two threads (each forms the line's pair sums itself), which
 // halves the registers a thread needs and doubles the warps that hide memory
-// latency; the FP64 body is bound by the FP64 pipe and keeps one.
-template <typename CT>
+// latency; below p = 3 a line has a single output pair, so one thread takes
+// it.  The FP64 body is bound by the FP64 pipe and keeps one.
+template <int P, typename CT>
 __host__ __device__ constexpr int eo_parts() {
-  return sizeof(CT) == 4 ? 2 : 1;
+  return (sizeof(CT) == 4 && P >= 3) ? 2 : 1;
 }
 
 template <int P, typename CT = double>
 struct EoCfg {
-  static constexpr int THREADS = 256 * eo_parts<CT>();
+  static constexpr int THREADS = 256 * eo_parts<P, CT>();
   static constexpr int EPB = (256 / Ord<P>::NQ2) > 0 ? 256 / Ord<P>::NQ2 : 1;
 };
 
@@ -98,7 +99,7 @@ template <int P, typename CT, bool FLY = false>
 __host__ __device__ constexpr size_t eo_block_smem(int nloc) {
   using O = Ord<P>;
   constexpr int arrays =
-      sizeof(CT) == 8 ? 1 : (eo_stages_q<CT>() ? 2 : 1) + (FLY ? 0 : 2) + (eo_parts<CT>() > 1 ? 1 : 0);
+      sizeof(CT) == 8 ? 1 : (eo_stages_q<CT>() ? 2 : 1) + (FLY ? 0 : 2) + (eo_parts<P, CT>() > 1 ? 1 : 0);
   return sizeof(CT) * (size_t)(3 * EoShape<P>::TE + nloc * (arrays * O::NP + O::NFT)) +
          sizeof(int) * 6 * (size_t)nloc;
 }
@@ -225,9 +226,9 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   constexpr bool kSYZ = !kF64 && !FLY;    // F_y, F_z staged (FP32 only)
   CT* sFy = sFx + (kSYZ ? nloc * NP : 0);
   CT* sFz = sFy + (kSYZ ? nloc * NP : 0);
-  constexpr int PARTS = eo_parts<CT>();
+  constexpr int PARTS = eo_parts<P, CT>();
   CT* sAcc = (PARTS > 1) ? sFz + nloc * NP : sFx;  // line-result sums
-  CT* sf = sAcc + nloc * NP;
+  CT* sf = ((PARTS > 1) ? sAcc : sFz) + nloc * NP;   // after the last array
   int* snb = reinterpret_cast<int*>(sf + nloc * NFT);
 
   const double* __restrict__ qin = a.q_in;
@@ -410,16 +411,16 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   });
 }
 
-// Resident blocks an SM.  FP32 (512 threads): the body issues few
-// instructions per byte and needs warps to hide memory latency, so up to
-// p = 12 the registers are capped at 32 for four blocks (64 warps; measured
-// 1.0-1.16x the three-block build, 100 against 91.5 GDOF-updates/s at p = 7);
-// above that shared memory admits three and the cap would only spill.
+// Resident blocks an SM.  FP32 (512 threads, 256 below p = 3): the body
+// issues few instructions per byte and needs warps to hide memory latency, so
+// up to p = 12 the registers are capped at 32 for 64 warps (measured 1.0-1.16x
+// the three-block build, 100 against 91.5 GDOF-updates/s at p = 7); above
+// that shared memory admits three blocks and the cap would only spill.
 // FP64: four blocks of 256 threads (registers capped at 64): a block in its
 // load or flux phase leaves three others feeding the FP64 pipe.
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_min_blocks() {
-  return sizeof(CT) == 8 ? 4 : (P <= 12 ? 4 : 3);
+  return sizeof(CT) == 8 ? 4 : (P <= 2 ? 8 : P <= 12 ? 4 : 3);
 }
 
 // FP32 single-box kernel: F_y / F_z formed on the fly (FLY) at the orders

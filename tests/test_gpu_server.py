@@ -89,14 +89,14 @@ def test_launch_shape_does_not_change_results(ops):
             assert np.array_equal(a, b)
 
 
-def test_default_body_is_the_node_body_at_p2_and_even_odd_above(ops):
+def test_default_body_is_the_even_odd_body(ops):
     rs = {2: req((3, 2, 2), 2, 9, 61), 5: req((2, 3, 2), 5, 9, 62)}
     got = {}
     for name, opt in (("default", 0), ("node", sdg.OPT_GENERAL), ("evenodd", sdg.OPT_EVENODD)):
         srv = sdg.Server(ops, opt=opt)
         got[name] = {p: srv.wait(srv.submit(**r, want_state=True))[1] for p, r in rs.items()}
         srv.close()
-    assert np.array_equal(got["default"][2], got["node"][2])
+    assert np.array_equal(got["default"][2], got["evenodd"][2])
     assert np.array_equal(got["default"][5], got["evenodd"][5])
     assert not np.array_equal(got["node"][5], got["evenodd"][5])
 
