@@ -62,11 +62,13 @@ struct EoShape {
 // Threads per line in the line phases: the FP32 body splits a line's output
 // pairs between two threads (each forms the line's pair sums itself), which
 // halves the registers a thread needs and doubles the warps that hide memory
-// latency; below p = 3 a line has a single output pair, so one thread takes
-// it.  The FP64 body is bound by the FP64 pipe and keeps one.
+// latency; at low orders a line has one or two output pairs, and one thread
+// a line measured faster on GB300 up to p = 3 in the single-box kernel (p = 3:
+// 91.8 against 72.5 GDOF-updates/s).  The FP64 body is bound by the FP64 pipe
+// and keeps one.  The batched kernels pick their own count (batch_eo_parts).
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_parts() {
-  return (sizeof(CT) == 4 && P >= 3) ? 2 : 1;
+  return (sizeof(CT) == 4 && P >= 4) ? 2 : 1;
 }
 
 template <int P, typename CT = double>
@@ -95,11 +97,12 @@ __host__ __device__ constexpr bool eo_stages_q() {
 // F = q v / q w from the staged q and the velocity in cache: two arrays less,
 // which keeps more blocks resident at high orders, for two extra velocity
 // reads per line node.
-template <int P, typename CT, bool FLY = false>
+template <int P, typename CT, bool FLY = false, int PARTS_SET = 0>
 __host__ __device__ constexpr size_t eo_block_smem(int nloc) {
   using O = Ord<P>;
+  constexpr int parts = PARTS_SET > 0 ? PARTS_SET : eo_parts<P, CT>();
   constexpr int arrays =
-      sizeof(CT) == 8 ? 1 : (eo_stages_q<CT>() ? 2 : 1) + (FLY ? 0 : 2) + (eo_parts<P, CT>() > 1 ? 1 : 0);
+      sizeof(CT) == 8 ? 1 : (eo_stages_q<CT>() ? 2 : 1) + (FLY ? 0 : 2) + (parts > 1 ? 1 : 0);
   return sizeof(CT) * (size_t)(3 * EoShape<P>::TE + nloc * (arrays * O::NP + O::NFT)) +
          sizeof(int) * 6 * (size_t)nloc;
 }
@@ -210,7 +213,8 @@ __device__ __forceinline__ void eo_pairs_f64(const double* __restrict__ q,
 // loop by 4, so more loads are in flight per warp.  Measured on GB300 for the
 // single-box kernel: 1.03-1.06x at p >= 4 (103 GDOF-updates/s at p = 7),
 // 0.95x at p = 1; in the batched kernel it was 0.8-0.9x, so it stays off there.
-template <int P, typename CT, int RKFIX = -1, bool FLY = false, bool PREF = false>
+template <int P, typename CT, int RKFIX = -1, bool FLY = false, bool PREF = false,
+          int PARTS_SET = 0>
 __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb, int nloc,
                                                unsigned char* smem) {
   using O = Ord<P>;
@@ -226,7 +230,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   constexpr bool kSYZ = !kF64 && !FLY;    // F_y, F_z staged (FP32 only)
   CT* sFy = sFx + (kSYZ ? nloc * NP : 0);
   CT* sFz = sFy + (kSYZ ? nloc * NP : 0);
-  constexpr int PARTS = eo_parts<P, CT>();
+  constexpr int PARTS = PARTS_SET > 0 ? PARTS_SET : eo_parts<P, CT>();
   CT* sAcc = (PARTS > 1) ? sFz + nloc * NP : sFx;  // line-result sums
   CT* sf = ((PARTS > 1) ? sAcc : sFz) + nloc * NP;   // after the last array
   int* snb = reinterpret_cast<int*>(sf + nloc * NFT);
@@ -411,7 +415,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   });
 }
 
-// Resident blocks an SM.  FP32 (512 threads, 256 below p = 3): the body
+// Resident blocks an SM.  FP32 (512 threads, 256 up to p = 3): the body
 // issues few instructions per byte and needs warps to hide memory latency, so
 // up to p = 12 the registers are capped at 32 for 64 warps (measured 1.0-1.16x
 // the three-block build, 100 against 91.5 GDOF-updates/s at p = 7); above
@@ -420,7 +424,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
 // load or flux phase leaves three others feeding the FP64 pipe.
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_min_blocks() {
-  return sizeof(CT) == 8 ? 4 : (P <= 2 ? 8 : P <= 12 ? 4 : 3);
+  return sizeof(CT) == 8 ? 4 : (P <= 3 ? 8 : P <= 12 ? 4 : 3);
 }
 
 // FP32 single-box kernel: F_y / F_z formed on the fly (FLY) at the orders
