@@ -71,10 +71,19 @@ __host__ __device__ constexpr int eo_parts() {
   return (sizeof(CT) == 4 && P >= 4) ? 2 : 1;
 }
 
+// Lines of a block: 256, or 128 for the FP32 body at p = 7, 9 and 10, where
+// twice as many half-size blocks (the same 64 warps an SM) measured 1.04-1.05x
+// on GB300 (108 against 103 GDOF-updates/s at p = 7; 0.95x at p = 8).
+template <int P, typename CT>
+__host__ __device__ constexpr int eo_lines() {
+  return (sizeof(CT) == 4 && (P == 7 || P == 9 || P == 10)) ? 128 : 256;
+}
+
 template <int P, typename CT = double>
 struct EoCfg {
-  static constexpr int THREADS = 256 * eo_parts<P, CT>();
-  static constexpr int EPB = (256 / Ord<P>::NQ2) > 0 ? 256 / Ord<P>::NQ2 : 1;
+  static constexpr int LINES = eo_lines<P, CT>();
+  static constexpr int THREADS = LINES * eo_parts<P, CT>();
+  static constexpr int EPB = (LINES / Ord<P>::NQ2) > 0 ? LINES / Ord<P>::NQ2 : 1;
 };
 
 // Dynamic shared memory of one block with nloc elements: the three scaled
@@ -415,7 +424,8 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   });
 }
 
-// Resident blocks an SM.  FP32 (512 threads, 256 up to p = 3): the body
+// Resident blocks an SM.  FP32 (512 threads; 256 up to p = 3 and at p = 7,
+// 9, 10, with twice the blocks): the body
 // issues few instructions per byte and needs warps to hide memory latency, so
 // up to p = 12 the registers are capped at 32 for 64 warps (measured 1.0-1.16x
 // the three-block build, 100 against 91.5 GDOF-updates/s at p = 7); above
@@ -424,7 +434,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
 // load or flux phase leaves three others feeding the FP64 pipe.
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_min_blocks() {
-  return sizeof(CT) == 8 ? 4 : (P <= 3 ? 8 : P <= 12 ? 4 : 3);
+  return sizeof(CT) == 8 ? 4 : (P <= 3 || eo_lines<P, CT>() == 128) ? 8 : P <= 12 ? 4 : 3;
 }
 
 // FP32 single-box kernel: F_y / F_z formed on the fly (FLY) at the orders
