@@ -13,9 +13,10 @@ with pinned host buffers (upload q,u,v,w, one step, download q, every step).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 With --impl reference the CPU oracle (a C + OpenMP restatement of the
-reference's Fortran path; the Fortran reference cannot be built here) is timed
-on the host cores on the same workload.  Under torchrun with N > 1 every rank
-runs an independent replica (the spec path is single-GPU); rank 0 prints.
+reference's Fortran path, which has no Fortran compiler to build it with) is
+timed on the host cores on the same workload.  Under torchrun with N > 1 every
+rank runs an independent replica (the path is built for one GPU and exchanges
+nothing between boxes); rank 0 prints.
 """
 from __future__ import annotations
 
