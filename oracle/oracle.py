@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check of
 __graft_entry__.py and by the cpu_baseline / reference arm of bench.py, as the
-parity checker or the timed CPU baseline.  The product library never imports
+oracle the parity tests compare against or the timed CPU baseline.  The product library never imports
 it.  Arrays follow the reference's Fortran column-major layout and are passed
 as flat numpy arrays (order='F' views are used for readability in tests).
 """

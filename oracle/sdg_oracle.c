@@ -1,7 +1,7 @@
 /*
  * sdg_oracle.c -- CPU restatement of the SCALE-DG kernel-extraction hot path
  * (advection tendency, DG operators, halo update, SSP-RK3), used ONLY as the
- * parity checker and as the timed CPU baseline.  See sdg_oracle.h for the
+ * oracle of the parity tests and as the timed CPU baseline.  See sdg_oracle.h for the
  * parity status and conventions.  Every function cites the reference
  * file:line it restates; the loop and summation order follow the reference
  * so that results agree to rounding.

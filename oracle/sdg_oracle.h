@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This is the parity oracle: tests/, the smoke
  * check in __graft_entry__.py and the cpu_baseline / reference arm of
- * bench.py may call it, as the checker.  The GB300 product library never
+ * bench.py may call it, to compare against.  The GB300 product library never
  * links, loads or calls it.
  *
  * Parity status: the reference is Fortran and no Fortran compiler is
