@@ -1,15 +1,16 @@
 // Batched advance of many independent boxes (an ensemble, or the requests a
-// server holds) with one persistent launch per order present and RK stage.
+// server holds) with one launch per order present and RK stage.
 //
 // Every box is an instance with its own order p, size, dt, rotating state
 // buffers and velocity.  A work item is one block's worth of consecutive
 // elements of one instance.  The item list is sorted by order; each order's
-// items run in one persistent launch of a kernel compiled for that order,
-// whose blocks take items round-robin, prefetch the next item's instance
-// header into shared memory while computing the current one, resolve the
-// instance's buffers for the stage, and run the same fused stage body as the
-// single-box solver (stage_block or stage_eo_block, FP32 compute, FP64
-// state).  Each instance's current
+// items run in one launch of a kernel compiled for that order and body:
+// one block per item for the even-odd body (batch_one_item), or persistent
+// blocks that take items round-robin and prefetch the next item's instance
+// header into shared memory while computing the current one.  A block
+// resolves the instance's buffers for the stage and runs the same fused
+// stage body as the single-box solver (stage_block or stage_eo_block, FP32
+// compute, FP64 state).  Each instance's current
 // buffer index lives on the device and is advanced by a tiny kernel after
 // stage 3, so one captured CUDA graph replays every step.
 #pragma once
@@ -61,15 +62,16 @@ inline void batch_stage_factors(BatchInst& I) {
   }
 }
 
-// The items of one order and stage body, run by one persistent launch of a
-// kernel compiled for that order and body.  The item list is sorted by order
+// The items of one order and stage body, run by one launch of a kernel
+// compiled for that order and body.  The item list is sorted by order
 // (and body), so a group is a contiguous range of it.
 struct BatchGroup {
   int p = 0, eo = 0;       // order, 1 for the even-odd body
   int begin = 0, count = 0;  // item range
   int threads = 256;       // block size
   size_t smem = 0;         // dynamic shared memory of a block
-  int grid = 0;            // persistent blocks (resident blocks, at most count)
+  int grid = 0;            // blocks: one per item (one-item kernel) or the
+                           // resident blocks, at most count (persistent kernel)
 };
 
 // Default block size and elements per work item of order p (1..11): the

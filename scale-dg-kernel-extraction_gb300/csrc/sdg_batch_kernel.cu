@@ -51,6 +51,73 @@ __host__ __device__ constexpr int batch_eo_parts() {
   return P <= 4 ? 1 : 2;
 }
 
+// One work item through one stage: the instance's buffers for the stage from
+// its current index, then the order's stage body.
+template <int P, int EO, int RK>
+__device__ __forceinline__ void batch_item_body(const BatchInst& I, const BatchItem& w,
+                                                int stage, unsigned char* smem) {
+  const int s0 = I.cur, s1 = (s0 + 1) % 3, s2 = (s0 + 2) % 3;
+  StageArgs a;
+  a.q_in = (stage == 0) ? I.q[s0] : (stage == 1) ? I.q[s1] : I.q[s2];
+  a.q0 = (stage == 0) ? nullptr : I.q[s0];
+  a.q_out = (stage == 1) ? I.q[s2] : I.q[s1];
+  a.u = I.u;
+  a.v = I.v;
+  a.w = I.w;
+  a.D = EO ? static_cast<const void*>(I.eo_tab) : static_cast<const void*>(I.D);
+  a.Lift = I.Lift;
+  a.box = I.box;
+  a.elem_begin = 0;
+  a.elem_count = I.box.Ne;
+  a.a = c_rk_a[stage];
+  a.b = c_rk_b[stage];
+  a.dt = I.dt;
+  a.cdt_hi = I.cdt[stage];  // FP32 increment factor of the FP32 form
+  a.cdt_lo = 0.0f;
+  a.b_is_one = (stage == 0);
+  a.a_nonzero = (stage != 0);
+  a.tend_only = 0;
+  if constexpr (EO != 0) {
+    for (int d = 0; d < 3; d++) {
+      a.eo_sDf[d] = I.eo_sD[stage][d];
+      a.eo_sLf[d] = I.eo_sL[stage][d];
+    }
+    stage_eo_block<P, float, RK, batch_eo_fly<P>(), false, batch_eo_parts<P>()>(
+        a, w.e_begin, w.e_count, smem);
+  } else {
+    stage_block<P, float, float, false, RK>(a, w.e_begin, w.e_count, smem);
+  }
+}
+
+// One block per work item, no loop: no work-item state stays live across
+// the stage body, so the body keeps the registers the persistent form
+// spends on its prefetch pipeline (the persistent kernel spilled 40-48 bytes
+// at p = 7 under the 32-register cap).  Measured on GB300 for the even-odd
+// body: 1.03-1.15x at every order but p = 8 (p = 7: 103.5 against 89.9
+// GDOF-updates/s), 0.97x at p = 8; the node body is faster persistent.
+template <int P, int EO>
+__host__ __device__ constexpr bool batch_one_item() {
+  return EO != 0 && P != 8;
+}
+
+template <int P, int EO, int RK>
+__global__ void __launch_bounds__(kBatchThreadsMax, batch_min_blocks<P, EO>())
+    batch_item_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
+                      int n_items, int stage) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ __align__(16) BatchInst s_inst;
+  __shared__ BatchItem s_item;
+  const int tid = threadIdx.x;
+  if ((int)blockIdx.x >= n_items) return;  // uniform across the block
+  if (tid == 0) s_item = items[blockIdx.x];
+  __syncthreads();
+  if (tid < kInstWords)
+    reinterpret_cast<uint32_t*>(&s_inst)[tid] =
+        reinterpret_cast<const uint32_t*>(insts + s_item.inst)[tid];
+  __syncthreads();
+  if (s_inst.active) batch_item_body<P, EO, RK>(s_inst, s_item, stage, smem);
+}
+
 template <int P, int EO, int RK>
 __global__ void __launch_bounds__(kBatchThreadsMax, batch_min_blocks<P, EO>())
     batch_order_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
@@ -85,39 +152,7 @@ __global__ void __launch_bounds__(kBatchThreadsMax, batch_min_blocks<P, EO>())
 
     const BatchItem w = s_items[slot];
     const BatchInst& I = s_inst[slot];
-    if (I.active) {
-      const int s0 = I.cur, s1 = (s0 + 1) % 3, s2 = (s0 + 2) % 3;
-      StageArgs a;
-      a.q_in = (stage == 0) ? I.q[s0] : (stage == 1) ? I.q[s1] : I.q[s2];
-      a.q0 = (stage == 0) ? nullptr : I.q[s0];
-      a.q_out = (stage == 1) ? I.q[s2] : I.q[s1];
-      a.u = I.u;
-      a.v = I.v;
-      a.w = I.w;
-      a.D = EO ? static_cast<const void*>(I.eo_tab) : static_cast<const void*>(I.D);
-      a.Lift = I.Lift;
-      a.box = I.box;
-      a.elem_begin = 0;
-      a.elem_count = I.box.Ne;
-      a.a = c_rk_a[stage];
-      a.b = c_rk_b[stage];
-      a.dt = I.dt;
-      a.cdt_hi = I.cdt[stage];  // FP32 increment factor of the FP32 form
-      a.cdt_lo = 0.0f;
-      a.b_is_one = (stage == 0);
-      a.a_nonzero = (stage != 0);
-      a.tend_only = 0;
-      if constexpr (EO != 0) {
-        for (int d = 0; d < 3; d++) {
-          a.eo_sDf[d] = I.eo_sD[stage][d];
-          a.eo_sLf[d] = I.eo_sL[stage][d];
-        }
-        stage_eo_block<P, float, RK, batch_eo_fly<P>(), false, batch_eo_parts<P>()>(
-            a, w.e_begin, w.e_count, smem);
-      } else {
-        stage_block<P, float, float, false, RK>(a, w.e_begin, w.e_count, smem);
-      }
-    }
+    if (I.active) batch_item_body<P, EO, RK>(I, w, stage, smem);
     // every read of this item's slots happened before the body's barriers
     __syncthreads();
     if (has_next && tid < kInstWords) reinterpret_cast<uint32_t*>(&s_inst[slot ^ 1])[tid] = hw;
@@ -189,11 +224,18 @@ namespace {
 // The three functions an order group needs, for one (P, EO) pair.
 template <int P, int EO>
 struct GroupOps {
+  static constexpr bool kOneItem = batch_one_item<P, EO>();
   static int set_smem(size_t smem) {
     SDG_CUDA_TRY(cudaFuncSetAttribute(batch_order_kernel<P, EO, kRkFirst>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     SDG_CUDA_TRY(cudaFuncSetAttribute(batch_order_kernel<P, EO, kRkGeneral>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if constexpr (kOneItem) {
+      SDG_CUDA_TRY(cudaFuncSetAttribute(batch_item_kernel<P, EO, kRkFirst>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      SDG_CUDA_TRY(cudaFuncSetAttribute(batch_item_kernel<P, EO, kRkGeneral>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
     return SDG_OK;
   }
   static int blocks_per_sm(int threads, size_t smem) {
@@ -207,6 +249,16 @@ struct GroupOps {
   }
   static int launch(const BatchInst* d_inst, const BatchItem* d_items, int n, int stage,
                     int grid, int threads, size_t smem, cudaStream_t st) {
+    if constexpr (kOneItem) {
+      if (stage == 0)
+        batch_item_kernel<P, EO, kRkFirst><<<grid, threads, smem, st>>>(d_inst, d_items, n,
+                                                                        stage);
+      else
+        batch_item_kernel<P, EO, kRkGeneral><<<grid, threads, smem, st>>>(d_inst, d_items, n,
+                                                                          stage);
+      SDG_CUDA_TRY(cudaGetLastError());
+      return SDG_OK;
+    }
     if (stage == 0)
       batch_order_kernel<P, EO, kRkFirst><<<grid, threads, smem, st>>>(d_inst, d_items, n, stage);
     else
@@ -234,9 +286,9 @@ int with_group(int p, int eo, F&& f) {
 
 void batch_default_shape(int p, int* threads, int* epb) {
   // index = order; measured with sdg_ensemble_tune, block sizes 128/256/512
-  static const int kThreads[kBatchMaxOrder + 1] = {256, 128, 128, 128, 128, 256,
+  static const int kThreads[kBatchMaxOrder + 1] = {256, 128, 256, 128, 256, 256,
                                                    128, 512, 256, 256, 256, 512};
-  static const int kEpb[kBatchMaxOrder + 1] = {1, 64, 16, 8, 4, 4, 2, 4, 2, 1, 1, 1};
+  static const int kEpb[kBatchMaxOrder + 1] = {1, 64, 32, 8, 8, 4, 2, 4, 2, 1, 1, 1};
   const int i = (p >= 1 && p <= kBatchMaxOrder) ? p : 0;
   *threads = kThreads[i];
   *epb = kEpb[i];
@@ -250,10 +302,12 @@ int batch_group_setup(BatchGroup& g) {
   SDG_CUDA_TRY(cudaGetDevice(&dev));
   SDG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   int per_sm = 0;
+  bool one_item = false;
   const int st = with_group<GroupOps>(g.p, g.eo, [&](auto ops) {
     const int r = decltype(ops)::set_smem(g.smem);
     if (r != SDG_OK) return r;
     per_sm = decltype(ops)::blocks_per_sm(threads, g.smem);
+    one_item = decltype(ops)::kOneItem;
     return SDG_OK;
   });
   if (st != SDG_OK) return st;
@@ -261,7 +315,7 @@ int batch_group_setup(BatchGroup& g) {
     return fail(SDG_ERR_INVALID_ARG, "batch kernel of order %d does not fit: %d threads, %zu B",
                 g.p, threads, g.smem);
   const long long cap = (long long)nsm * per_sm;
-  g.grid = (int)(g.count < cap ? g.count : cap);
+  g.grid = one_item ? g.count : (int)(g.count < cap ? g.count : cap);
   return SDG_OK;
 }
 
