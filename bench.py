@@ -373,7 +373,7 @@ def bench_ensemble(sdg, args):
     return {
         "workload": f"{args.ens_n} instances, Ne per axis U{{4..24}}, p in {{3,5,7}}, "
                     f"sigma U[0.05,0.2], constant |u|<=1, {args.ens_steps} steps, "
-                    "FP32 compute / FP64 RK state, one persistent launch per order and stage, "
+                    "FP32 compute / FP64 RK state, one launch per order and stage, "
                     "CUDA graph",
         "total_dof": dof,
         "solves_per_s": args.ens_n / per_solve,

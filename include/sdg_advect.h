@@ -349,14 +349,13 @@ int sdg_solver_launches_per_step(const sdg_solver* s);
 void* sdg_solver_stream(const sdg_solver* s);
 int sdg_solver_destroy(sdg_solver* s);
 
-/* ---- batched ensembles: one persistent launch per RK stage ------------- */
+/* ---- batched ensembles: one launch per RK stage and order --------------- */
 
 /* Many independent periodic boxes (orders 1..11, any sizes, each with its own
  * dt) advanced together in FP32-compute / FP64-state form.  A step is a CUDA
- * graph of one persistent launch per RK stage and (order, stage body) group
- * (the blocks of a group take its (instance, element block) work items
- * round-robin; the groups run on parallel branches) and an index advance:
- * 3 x groups + 1 kernels.
+ * graph of one launch per RK stage and (order, stage body) group (one block
+ * per (instance, element block) work item, or persistent blocks that take
+ * the items round-robin) and an index advance: 3 x groups + 1 kernels.
  * dims holds NeX,NeY,NeZ per instance; D1D_by_order / Lift_by_order /
  * x1D_by_order are indexed by the order (entries for absent orders may be
  * NULL; x1D_by_order may be NULL when sdg_ensemble_init_blob is not used).
@@ -399,7 +398,7 @@ int sdg_ensemble_set_parallel_groups(sdg_ensemble* e, int on);
 int sdg_ensemble_get_bodies(const sdg_ensemble* e, int* eo_by_order);
 /* epb_by_order receives 12 entries (index = order); threads the block size
  * the present orders share (0 when they differ); grid the largest group's
- * persistent grid. */
+ * grid. */
 int sdg_ensemble_get_config(const sdg_ensemble* e, int* epb_by_order,
                             int* threads, int* grid);
 int sdg_ensemble_step(sdg_ensemble* e, int nstep);
@@ -415,7 +414,7 @@ int sdg_ensemble_destroy(sdg_ensemble* e);
  * order 1..11, size, dt and step count, and a Gaussian tracer in a constant
  * velocity generated on the device) are admitted while the HBM budget and the
  * slot count allow; every active request advances one SSP-RK3 step per
- * round of batched persistent launches (FP32 compute, FP64 state), so
+ * round of batched launches (FP32 compute, FP64 state), so
  * requests that arrive while others run share the GPU from their next step
  * on.  Finished requests release their memory at once.  No reference
  * counterpart: the reference runs one box per process. */

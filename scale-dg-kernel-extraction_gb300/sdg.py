@@ -475,7 +475,7 @@ class Solver:
 
 
 class Ensemble:
-    """Independent boxes advanced together, one persistent launch per order and
+    """Independent boxes advanced together, one launch per order and
     RK stage (sdg_ensemble_* in include/sdg_advect.h); FP32 compute, FP64
     state."""
 
