@@ -28,11 +28,11 @@ static_assert(kInstWords < 128, "the smallest block must copy the header in one 
 // Resident blocks of 512 threads an SM the registers are capped for: 4 (32
 // registers) where that measured faster on GB300, else 3 (40 registers).
 // The node body gains 4-16 % from the fourth block at every order; the
-// even-odd body at p = 1, 5, 7, 8, 9 and 11 (up to 22 % at p = 11) and loses
-// up to 10 % at p = 2, 3, 4, 6 and 10, where the cap spills.
+// even-odd body, in its one-item kernel, up to 15 % (p = 2, 3) at every order
+// but p = 10 (0.92x there).
 template <int P, int EO>
 __host__ __device__ constexpr int batch_min_blocks() {
-  return (EO == 0 || P == 1 || P == 5 || P == 7 || P == 8 || P == 9 || P == 11) ? 4 : 3;
+  return (EO != 0 && P == 10) ? 3 : 4;
 }
 
 // Even-odd body: F_y / F_z formed on the fly rather than staged at the orders
@@ -286,9 +286,9 @@ int with_group(int p, int eo, F&& f) {
 
 void batch_default_shape(int p, int* threads, int* epb) {
   // index = order; measured with sdg_ensemble_tune, block sizes 128/256/512
-  static const int kThreads[kBatchMaxOrder + 1] = {256, 128, 256, 128, 256, 256,
-                                                   128, 512, 256, 256, 256, 512};
-  static const int kEpb[kBatchMaxOrder + 1] = {1, 64, 32, 8, 8, 4, 2, 4, 2, 1, 1, 1};
+  static const int kThreads[kBatchMaxOrder + 1] = {256, 128, 256, 256, 256, 256,
+                                                   256, 512, 256, 256, 256, 512};
+  static const int kEpb[kBatchMaxOrder + 1] = {1, 64, 32, 16, 8, 4, 4, 4, 2, 1, 1, 1};
   const int i = (p >= 1 && p <= kBatchMaxOrder) ? p : 0;
   *threads = kThreads[i];
   *epb = kEpb[i];
