@@ -79,11 +79,15 @@ __host__ __device__ constexpr int eo_lines() {
   return (sizeof(CT) == 4 && (P == 7 || P == 9 || P == 10)) ? 128 : 256;
 }
 
+// The FP32 body at p = 5 runs 4 elements (144 lines, two threads a line) on
+// 256 threads, eight blocks an SM: 1.07x the 512-thread shape (79.1 against
+// 73.6 GDOF-updates/s); the same at p = 4 and 6 was level or slower.
 template <int P, typename CT = double>
 struct EoCfg {
+  static constexpr bool SMALL5 = sizeof(CT) == 4 && P == 5;
   static constexpr int LINES = eo_lines<P, CT>();
-  static constexpr int THREADS = LINES * eo_parts<P, CT>();
-  static constexpr int EPB = (LINES / Ord<P>::NQ2) > 0 ? LINES / Ord<P>::NQ2 : 1;
+  static constexpr int THREADS = SMALL5 ? 256 : LINES * eo_parts<P, CT>();
+  static constexpr int EPB = SMALL5 ? 4 : (LINES / Ord<P>::NQ2) > 0 ? LINES / Ord<P>::NQ2 : 1;
 };
 
 // Dynamic shared memory of one block with nloc elements: the three scaled
@@ -434,7 +438,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
 // load or flux phase leaves three others feeding the FP64 pipe.
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_min_blocks() {
-  return sizeof(CT) == 8 ? 4 : (P <= 3 || eo_lines<P, CT>() == 128) ? 8 : P <= 12 ? 4 : 3;
+  return sizeof(CT) == 8 ? 4 : (P <= 3 || P == 5 || eo_lines<P, CT>() == 128) ? 8 : P <= 12 ? 4 : 3;
 }
 
 // FP32 single-box kernel: F_y / F_z formed on the fly (FLY) at the orders
