@@ -40,7 +40,7 @@ extern "C" {
 #define SDG_OK 0
 #define SDG_ERR_INVALID_ARG (-1)   /* bad size, NULL pointer, bad stage ... */
 #define SDG_ERR_UNSUPPORTED_ORDER (-2) /* PolyOrder outside 1..15 */
-#define SDG_ERR_BAD_OPTTYPE (-3)   /* not "GENERAL" / "OPT1", or never set */
+#define SDG_ERR_BAD_OPTTYPE (-3)   /* not "GENERAL" / "OPT1" / "EVENODD", or never set */
 #define SDG_ERR_CUDA (-4)          /* a CUDA runtime call failed */
 #define SDG_ERR_OUT_OF_MEMORY (-5) /* device or host allocation failed */
 #define SDG_ERR_FILE (-6)          /* operator file missing or malformed */
@@ -51,11 +51,11 @@ extern "C" {
 /* DGOptrKernel optimisation types (mod_dg_optr_kernel.f90:38-42). */
 #define SDG_OPT_GENERAL 1
 #define SDG_OPT_OPT1 2
-/* Solver and batched forms only: the stage with the even-odd factorisation
- * of D1D and of the face lift (needs their centro-symmetry, which GLL
- * operators have to rounding); ~30 % fewer FP64 operations in the FP64 form,
- * about half the instructions in the FP32 and emulated forms, same result to
- * rounding. */
+/* The even-odd factorisation of D1D and of the face lift (needs their
+ * centro-symmetry, which GLL operators have to rounding): in the solver and
+ * batched forms the fused stage with ~30 % fewer FP64 operations in the FP64
+ * form and about half the instructions in the FP32 and emulated forms; in
+ * cal_tend the even-odd tendency kernel.  Same result to rounding. */
 #define SDG_OPT_EVENODD 3
 
 /* Arithmetic of a solver (the reference is FP64 throughout). */
