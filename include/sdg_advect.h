@@ -96,6 +96,15 @@ int sdg_operator_read(const char* path, int p, double* x1D, double* D1D,
  * agree with operator_data/p*.dat to rounding.  D1D_tr may be NULL. */
 int sdg_operator_generate(int p, double* x1D, double* D1D, double* D1D_tr,
                           double* Lift_mat);
+/* The FP64 even-odd tables the EVENODD forms build from an order's operators
+ * (host computation, no device): for each axis x, y, z, TE values
+ * E(i,l) (i,l < H), O(i,l) (i < HR, l < H), D(i,mid) (i < H, odd N only),
+ * A(i) (i < HR), B(i) (i < H), with N = Nq, H = N/2, HR = (N+1)/2 and
+ * TE = H*H + HR*H + (N odd ? H : 0) + HR + H; `tables` receives 3*TE values,
+ * unscaled.  Returns SDG_ERR_INVALID_ARG when D1D is not centro-antisymmetric
+ * or Lift_mat not separable and mirrored (to 1e-13 of the largest entry). */
+int sdg_evenodd_tables(int Nq, const double* D1D, const double* Lift_mat,
+                       double* tables);
 
 /* ---- drop-in for mod_dg_optr_kernel / mod_advect3d_eq ------------------ */
 

@@ -4,6 +4,7 @@
 
 #include <atomic>
 #include <cctype>
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -443,5 +444,15 @@ int sdg_dg_optr_kernel_setup(const char* t) {
 }
 
 int sdg_dg_optr_kernel_type(void) { return g_opttype.load(); }
+
+int sdg_evenodd_tables(int Nq, const double* D1D, const double* Lift_mat, double* tables) {
+  if (!D1D || !Lift_mat || !tables) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  if (Nq - 1 < 1 || Nq - 1 > kMaxOrder)
+    return fail(SDG_ERR_UNSUPPORTED_ORDER, "PolyOrder %d outside 1..15", Nq - 1);
+  std::vector<double> tab;
+  SDG_TRY(eo_tables(Nq, D1D, Lift_mat, tab));
+  std::copy(tab.begin(), tab.end(), tables);
+  return SDG_OK;
+}
 
 }  // extern "C"

@@ -93,6 +93,7 @@ def _load() -> C.CDLL:
         "sdg_set_device": ([_i], _i),
         "sdg_operator_read": ([C.c_char_p, _i, _dp, _dp, _vp, _dp], _i),
         "sdg_operator_generate": ([_i, _dp, _dp, _vp, _dp], _i),
+        "sdg_evenodd_tables": ([_i, _dp, _dp, _dp], _i),
         "sdg_dg_optr_kernel_setup": ([C.c_char_p], _i),
         "sdg_dg_optr_kernel_type": ([], _i),
         "sdg_advect3d_eq_cal_tend": ([_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip,
@@ -221,6 +222,16 @@ def operator_generate(p: int):
     x, D, Dt, L = np.zeros(Nq), np.zeros(Nq * Nq), np.zeros(Nq * Nq), np.zeros(6 * Nq ** 3)
     _check(lib.sdg_operator_generate(p, x, D, Dt.ctypes.data, L), "sdg_operator_generate")
     return x, D, Dt, L
+
+
+def evenodd_tables(Nq: int, D1D, Lift_mat) -> np.ndarray:
+    """The even-odd tables of an order (3 x TE values; see sdg_advect.h)."""
+    N = Nq
+    H, HR, odd = N // 2, (N + 1) // 2, N & 1
+    te = H * H + HR * H + odd * H + HR + H
+    out = np.zeros(3 * te)
+    _check(lib.sdg_evenodd_tables(Nq, _f64(D1D), _f64(Lift_mat), out), "sdg_evenodd_tables")
+    return out
 
 
 # ---- the reference's entry points ------------------------------------------
