@@ -1,11 +1,14 @@
 """CPU tests of the even-odd tables the EVENODD forms build on the host: with
 them, the pair sums reproduce D1D applied to any line and the lift of the
 line's two faces, and operators without the symmetries are refused."""
+import os
+
 import numpy as np
 import pytest
 
+import oracle as O
 import sdg
-from helpers import operators
+from helpers import REF_OPDATA, operators
 
 
 def apply_tables(tab, N, F, gm, gp):
@@ -31,9 +34,7 @@ def apply_tables(tab, N, F, gm, gp):
     return out
 
 
-@pytest.mark.parametrize("p", range(1, 16))
-def test_tables_reproduce_derivative_and_lift(p):
-    x, D, Dt, L = operators(p)
+def check_tables(p, D, L):
     N = p + 1
     H, HR, odd = N // 2, (N + 1) // 2, N & 1
     te = H * H + HR * H + odd * H + HR + H
@@ -55,6 +56,21 @@ def test_tables_reproduce_derivative_and_lift(p):
             got = apply_tables(t, N, F, gm, gp)
             scale = np.abs(Dm).sum(axis=1).max() * np.abs(F).max() + np.abs(lam_m).max()
             assert np.max(np.abs(got - want)) <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("p", range(1, 16))
+def test_tables_reproduce_derivative_and_lift(p):
+    x, D, Dt, L = operators(p)
+    check_tables(p, D, L)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_OPDATA), reason="reference operator_data not mounted")
+@pytest.mark.parametrize("p", range(1, 16))
+def test_tables_of_the_reference_operator_files(p):
+    """The reference's operator files have the symmetries to 2.4e-14 (p = 15):
+    the tables build from them and reproduce their D1D and lift columns."""
+    x, D, Dt, L = O.read_operator_file(os.path.join(REF_OPDATA, f"p{p}.dat"), p)
+    check_tables(p, D, L)
 
 
 def test_tables_refuse_operators_without_the_symmetries():
