@@ -38,6 +38,14 @@ sys.path.insert(0, PKG)
 # algorithmic bytes per DOF-update: stage 1 reads q,u,v,w and writes q (40 B);
 # stages 2 and 3 also read q0 (48 B).  FP32 form: velocity in FP32.
 BYTES_PER_DOF_UPDATE = {"fp64": 136.0 / 3.0, "fp64emu": 136.0 / 3.0, "fp32": 100.0 / 3.0}
+
+
+def face_factor_bytes(precision: str, opt: str, p: int) -> float:
+    """Bytes per DOF-update of the face-flux velocity factors the even-odd FP64
+    and emulated-FP64 stages share within a step: stage 1 writes (tP, tM) for
+    the 6 Nq^2 face nodes of each element (96/Nq B a DOF), stages 2 and 3 read
+    them, so every launch moves 96/Nq B a DOF."""
+    return 96.0 / (p + 1) if opt == "evenodd" and precision in ("fp64", "fp64emu") else 0.0
 PRECISIONS = {"fp64": 0, "fp32": 1, "fp64emu": 2}
 
 
@@ -258,7 +266,7 @@ def time_solver(sdg, wl, p, ne, prec, steps, warmup, local, barrier, sample_cloc
 def roofline(precision, p, ne, ndof, t, steps, peaks, opt="opt1"):
     launches = 3 * steps
     avg_launch = t / launches
-    bpd = BYTES_PER_DOF_UPDATE[precision]
+    bpd = BYTES_PER_DOF_UPDATE[precision] + face_factor_bytes(precision, opt, p)
     achieved = bpd * ndof / avg_launch / 1e9
     peak, peak_kind = measured_peaks()
     per_gpu = ndof * 3 * steps / t / 1e9

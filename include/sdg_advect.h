@@ -299,7 +299,11 @@ typedef struct sdg_solver sdg_solver;
  * summation order of the divergence (they differ only for p > 7);
  * SDG_OPT_EVENODD the even-odd stage (returns SDG_ERR_INVALID_ARG if
  * D1D or Lift_mat lacks the centro-symmetry beyond 1e-13 relative).
- * precision = SDG_PREC_*.  stream may be NULL. */
+ * precision = SDG_PREC_*.  stream may be NULL.
+ * With SDG_OPT_EVENODD and SDG_PREC_FP64 or SDG_PREC_FP64_EMU the solver also
+ * holds the face-flux velocity factors of one step (16 bytes per face node,
+ * 96/Nq bytes per DOF): the first stage of every step forms them from the
+ * current velocity and the other two stages read them. */
 int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
                       double Lx, double Ly, double Lz, const double* D1D,
                       const double* Lift_mat, int opt, int precision,

@@ -67,6 +67,8 @@ __device__ __forceinline__ void batch_item_body(const BatchInst& I, const BatchI
   a.D = EO ? static_cast<const void*>(I.eo_tab) : static_cast<const void*>(I.D);
   a.Lift = I.Lift;
   a.box = I.box;
+  a.fc_out = nullptr;
+  a.fc_in = nullptr;
   a.elem_begin = 0;
   a.elem_count = I.box.Ne;
   a.a = c_rk_a[stage];

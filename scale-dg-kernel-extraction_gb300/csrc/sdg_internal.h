@@ -73,6 +73,13 @@ struct StageArgs {
   // D then points at the 3-direction table built by the solver
   double eo_sD[3], eo_sL[3];
   float eo_sDf[3], eo_sLf[3];  // the same factors for the FP32-compute form
+  // even-odd FP64 stage: the velocity factors of the face flux, (tP, tM) per
+  // face node of each element (2*Nfp*6 doubles an element).  A stage with
+  // fc_out forms them from u, v, w and stores them; a stage with fc_in reads
+  // them instead (same bits), so the three stages of one RK step, which share
+  // the velocity, form them once.  Both null: formed inline.
+  double* fc_out;
+  const double* fc_in;
 };
 
 // Even-odd tables (3 directions, unscaled) from D1D and Lift_mat after the

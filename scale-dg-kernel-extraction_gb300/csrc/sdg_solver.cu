@@ -36,6 +36,11 @@ struct sdg_solver {
   void* D = nullptr;
   void* Lift = nullptr;
   double* dqdt = nullptr;
+  // face-flux velocity factors shared by the three stages of a step (even-odd
+  // FP64 and emulated-FP64 stages; null otherwise): 96 / (p + 1) bytes a DOF.
+  // Measured on GB300 against forming them in every stage: 1.04-1.13x for the
+  // FP64 stage (p = 7: 19.3 against 18.5 GDOF-updates/s), 1.01-1.14x emulated.
+  double* fc = nullptr;
   // pipelined host-to-host solves (allocated on first use)
   IoSlot io[2];
   bool io_ready = false;
@@ -76,20 +81,24 @@ void release(sdg_solver* s) {
   cudaFree(s->D);
   cudaFree(s->Lift);
   cudaFree(s->dqdt);
+  cudaFree(s->fc);
 }
 
+// fc: 0 = the stage forms the face-flux velocity factors inline, 1 = it also
+// stores them in s->fc, 2 = it reads them from s->fc (a stage of the same
+// step, same velocity, stored them); 1 and 2 apply only when s->fc exists.
 int one_stage_on(sdg_solver* s, int stage, double dt, const double* qin, const double* q0,
                  double* qout, const void* u, const void* v, const void* w, cudaStream_t st,
-                 bool tend_only);
+                 bool tend_only, int fc = 0);
 
 int one_stage(sdg_solver* s, int stage, double dt, const double* qin,
-              const double* q0, double* qout, bool tend_only) {
-  return one_stage_on(s, stage, dt, qin, q0, qout, s->u, s->v, s->w, s->stream, tend_only);
+              const double* q0, double* qout, bool tend_only, int fc = 0) {
+  return one_stage_on(s, stage, dt, qin, q0, qout, s->u, s->v, s->w, s->stream, tend_only, fc);
 }
 
 int one_stage_on(sdg_solver* s, int stage, double dt, const double* qin, const double* q0,
                  double* qout, const void* u, const void* v, const void* w, cudaStream_t st,
-                 bool tend_only) {
+                 bool tend_only, int fc) {
   static const double rk_a[3] = {0.0, 0.75, 1.0 / 3.0};  // mod_common.f90:28-30
   static const double rk_b[3] = {1.0, 0.25, 2.0 / 3.0};
   StageArgs a{};
@@ -113,6 +122,8 @@ int one_stage_on(sdg_solver* s, int stage, double dt, const double* qin, const d
   a.b_is_one = (a.b == 1.0) ? 1 : 0;
   a.a_nonzero = (a.a != 0.0) ? 1 : 0;
   a.tend_only = tend_only ? 1 : 0;
+  a.fc_out = (s->fc && fc == 1) ? s->fc : nullptr;
+  a.fc_in = (s->fc && fc == 2) ? s->fc : nullptr;
   const double c = tend_only ? 1.0 : a.b * dt;
   for (int d = 0; d < 3; d++) {
     a.eo_sD[d] = -c * s->box.Es[d];
@@ -289,6 +300,8 @@ int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
   if (e == cudaSuccess) e = cudaMalloc(&s->w, es * (size_t)s->ndof);
   if (e == cudaSuccess) e = cudaMalloc(&s->D, dtab.size());
   if (e == cudaSuccess) e = cudaMalloc(&s->Lift, ltab.size());
+  if (e == cudaSuccess && precision != SDG_PREC_FP32 && opt == SDG_OPT_EVENODD)
+    e = cudaMalloc(&s->fc, 16 * (size_t)(6 * s->Nq * s->Nq) * (size_t)s->box.Ne);
   if (e == cudaSuccess) e = cudaMemcpy(s->D, dtab.data(), dtab.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(s->Lift, ltab.data(), ltab.size(), cudaMemcpyHostToDevice);
@@ -404,9 +417,9 @@ int sdg_solver_step(sdg_solver* s, double dt, int nstep) {
   if (nstep < 0) return fail(SDG_ERR_INVALID_ARG, "nstep < 0");
   for (int it = 0; it < nstep; it++) {
     const int s0 = s->cur, s1 = (s->cur + 1) % 3, s2 = (s->cur + 2) % 3;
-    SDG_TRY(one_stage(s, 0, dt, s->q[s0], nullptr, s->q[s1], false));
-    SDG_TRY(one_stage(s, 1, dt, s->q[s1], s->q[s0], s->q[s2], false));
-    SDG_TRY(one_stage(s, 2, dt, s->q[s2], s->q[s0], s->q[s1], false));
+    SDG_TRY(one_stage(s, 0, dt, s->q[s0], nullptr, s->q[s1], false, 1));
+    SDG_TRY(one_stage(s, 1, dt, s->q[s1], s->q[s0], s->q[s2], false, 2));
+    SDG_TRY(one_stage(s, 2, dt, s->q[s2], s->q[s0], s->q[s1], false, 2));
     s->cur = s1;
   }
   return SDG_OK;
@@ -556,9 +569,12 @@ int sdg_solver_solve_host_pipelined(sdg_solver* s, int count, const double* cons
     int cur = 0;
     for (int it = 0; it < nstep; it++) {
       const int s0 = cur, s1 = (cur + 1) % 3, s2 = (cur + 2) % 3;
-      SDG_TRY(one_stage_on(s, 0, dt, io.q[s0], nullptr, io.q[s1], io.u, io.v, io.w, s->comp, false));
-      SDG_TRY(one_stage_on(s, 1, dt, io.q[s1], io.q[s0], io.q[s2], io.u, io.v, io.w, s->comp, false));
-      SDG_TRY(one_stage_on(s, 2, dt, io.q[s2], io.q[s0], io.q[s1], io.u, io.v, io.w, s->comp, false));
+      SDG_TRY(one_stage_on(s, 0, dt, io.q[s0], nullptr, io.q[s1], io.u, io.v, io.w, s->comp,
+                           false, 1));
+      SDG_TRY(one_stage_on(s, 1, dt, io.q[s1], io.q[s0], io.q[s2], io.u, io.v, io.w, s->comp,
+                           false, 2));
+      SDG_TRY(one_stage_on(s, 2, dt, io.q[s2], io.q[s0], io.q[s1], io.u, io.v, io.w, s->comp,
+                           false, 2));
       cur = s1;
     }
     SDG_CUDA_TRY(cudaEventRecord(io.computed, s->comp));

@@ -218,7 +218,11 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS, emu_eo_min_blocks<P>())
   // normal sign through the constant +-2) and split once, g = F / 2 exactly.
   // Five FP64 operations a face node cost less than the two FP64 jumps, five
   // splits and two compensated products of the double-float form: that form
-  // issued about a fifth of the kernel's instructions.
+  // issued about a fifth of the kernel's instructions.  The velocity factors
+  // tP and tM come from fc_in when a stage before this one in the step
+  // stored them.
+  const double2* __restrict__ fcin = reinterpret_cast<const double2*>(a.fc_in);
+  double2* __restrict__ fcout = reinterpret_cast<double2*>(a.fc_out);
   for (int t = threadIdx.x; t < nloc * NFT; t += T) {
     const int le = t / NFT;
     const int r = t - le * NFT;
@@ -228,12 +232,21 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS, emu_eo_min_blocks<P>())
     face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sgi);
     const long long gM = g0 + (long long)le * NP + nM;
     const long long gP = (long long)snb[8 * le + f] * NP + nP;
-    const double* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
     const double qM = qin[gM], qP = qin[gP];
-    const double uM = gvel[gM], uP = gvel[gP];
-    const double a2 = abs_ct(uP + uM);
-    const double tw = (sgi > 0) ? 2.0 : -2.0;
-    const double tP = fma(tw, uP, -a2), tM = fma(tw, uM, -a2);
+    double tP, tM;
+    if (fcin != nullptr) {
+      const double2 c = fcin[eb * NFT + t];
+      tP = c.x;
+      tM = c.y;
+    } else {
+      const double* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
+      const double uM = gvel[gM], uP = gvel[gP];
+      const double a2 = abs_ct(uP + uM);
+      const double tw = (sgi > 0) ? 2.0 : -2.0;
+      tP = fma(tw, uP, -a2);
+      tM = fma(tw, uM, -a2);
+      if (fcout != nullptr) fcout[eb * NFT + t] = make_double2(tP, tM);
+    }
     const dfl gf = df_scale2(df_split(fma(qP, tP, -(qM * tM))), 0.5f);
     sg[t] = make_float2(gf.hi, gf.lo);
   }

@@ -27,6 +27,10 @@
 //  * The face flux 0.5 Fs (qP VelP - qM VelM - α (qP - qM)) is formed as
 //    qP (2VelP - 2α) - qM (2VelM - 2α) with 2α = |uP + uM| (the normal sign
 //    applied through the constant ±2): five FP64 operations per face node.
+//    Three of them form the velocity factors tP = ±2VelP - 2α and tM, which
+//    the three stages of a step share: the solver has its first stage store
+//    them (fc_out) and the other two read them (fc_in), two operations a face
+//    node there.
 //
 // Thread layout: phase 0 and the face flux run one thread per node / face
 // node as in stage_block; the three contraction phases run one thread per
@@ -316,7 +320,11 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   }
   __syncthreads();
 
-  // phase 1: face fluxes qP (2VelP - 2α) - qM (2VelM - 2α), unscaled
+  // phase 1: face fluxes qP (2VelP - 2α) - qM (2VelM - 2α), unscaled.  The
+  // velocity factors tP = ±2VelP - 2α and tM come from fc_in when a stage
+  // before this one in the step stored them (FP64 body).
+  const double2* __restrict__ fcin = reinterpret_cast<const double2*>(a.fc_in);
+  double2* __restrict__ fcout = reinterpret_cast<double2*>(a.fc_out);
   for (int t = threadIdx.x; t < nloc * NFT; t += T) {
     const int le = t / NFT;
     const int r = t - le * NFT;
@@ -326,18 +334,26 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
     face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sg);
     const long long gM = g0 + (long long)le * NP + nM;
     const long long gP = (long long)snb[6 * le + f] * NP + nP;
-    const CT* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
-    const CT uM = gvel[gM], uP = gvel[gP];
     CT qM;
     if constexpr (kSQ)
       qM = sq[le * NP + nM];
     else
       qM = to_ct<CT>(qin[gM]);
     const CT qP = to_ct<CT>(qin[gP]);
-    const CT a2 = abs_ct(uP + uM);
-    const CT tw = (sg > 0) ? CT(2) : CT(-2);
-    const CT tP = fma(tw, uP, -a2);
-    const CT tM = fma(tw, uM, -a2);
+    CT tP, tM;
+    if (kF64 && fcin != nullptr) {
+      const double2 c = fcin[eb * NFT + t];
+      tP = CT(c.x);
+      tM = CT(c.y);
+    } else {
+      const CT* gvel = (axis == 0) ? gu : (axis == 1) ? gv : gw;
+      const CT uM = gvel[gM], uP = gvel[gP];
+      const CT a2 = abs_ct(uP + uM);
+      const CT tw = (sg > 0) ? CT(2) : CT(-2);
+      tP = fma(tw, uP, -a2);
+      tM = fma(tw, uM, -a2);
+      if (kF64 && fcout != nullptr) fcout[eb * NFT + t] = make_double2(tP, tM);
+    }
     sf[le * NFT + r] = fma(qP, tP, -(qM * tM));
   }
   __syncthreads();

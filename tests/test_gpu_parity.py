@@ -135,9 +135,13 @@ def test_fp32_evenodd_tendency(p):
     assert rel_l2(dq, c.oracle_tend()) <= TOL_FP32
 
 
-@pytest.mark.parametrize("prec", [sdg.PREC_FP64, sdg.PREC_FP32, sdg.PREC_FP64_EMU])
+@pytest.mark.parametrize("prec,opt", [(sdg.PREC_FP64, sdg.OPT_OPT1),
+                                      (sdg.PREC_FP64, sdg.OPT_EVENODD),
+                                      (sdg.PREC_FP32, sdg.OPT_OPT1),
+                                      (sdg.PREC_FP64_EMU, sdg.OPT_OPT1),
+                                      (sdg.PREC_FP64_EMU, sdg.OPT_EVENODD)])
 @pytest.mark.parametrize("nstep", [1, 2, 3])
-def test_pipelined_host_solves_equal_plain_solves(prec, nstep):
+def test_pipelined_host_solves_equal_plain_solves(prec, opt, nstep):
     """Every result buffer (nstep % 3) and so every wait pattern of the
     two-slot pipeline; boxes large enough that copies overlap compute."""
     dims, p = (12, 10, 8), 5
@@ -147,14 +151,40 @@ def test_pipelined_host_solves_equal_plain_solves(prec, nstep):
     for c, pa in zip(cases, pins):
         for arr, src in zip(pa[:4], (c.q, c.u, c.v, c.w)):
             arr.array[:] = src[:n]
-    s = solver_for(cases[0], prec=prec)
+    s = solver_for(cases[0], opt=opt, prec=prec)
     s.solve_host_pipelined([pa[0].ptr for pa in pins], [pa[1].ptr for pa in pins],
                            [pa[2].ptr for pa in pins], [pa[3].ptr for pa in pins],
                            [pa[4].ptr for pa in pins], cases[0].dt, nstep)
     for c, pa in zip(cases, pins):
-        ref = solver_for(c, prec=prec)
+        ref = solver_for(c, opt=opt, prec=prec)
         ref.step(cases[0].dt, nstep)
         assert np.array_equal(pa[4].array, ref.download())
+
+
+@pytest.mark.parametrize("p", [5, 7, 11])
+@pytest.mark.parametrize("prec", [sdg.PREC_FP64, sdg.PREC_FP64_EMU])
+def test_evenodd_steps_follow_a_new_velocity(p, prec):
+    """The even-odd stages form the face-flux velocity factors in a step's
+    first stage and reuse them in its other two: a velocity uploaded between
+    steps must be the one the next step uses.  Checked against the node body
+    (which forms them in every stage) through a run whose velocity changes
+    sign and direction twice."""
+    c = Case(*mesh_dims(p), p, ic="blob")
+    n = c.nown
+    rng = np.random.default_rng(W.BASE_SEED + 70 + p)
+    vels = [(c.u[:n], c.v[:n], c.w[:n]),
+            (-0.5 * c.v[:n], 2.0 * c.w[:n], -c.u[:n]),
+            tuple(rng.uniform(-0.25, 0.25, n) for _ in range(3))]
+    out = []
+    for opt in (sdg.OPT_EVENODD, sdg.OPT_OPT1):
+        s = sdg.Solver(c.NeX, c.NeY, c.NeZ, p, c.D, c.Lift, opt=opt, precision=prec)
+        q = c.q[:n].copy()
+        for u, v, w in vels:
+            s.upload(q, u, v, w)
+            s.step(c.dt, 4)
+            q = s.download()
+        out.append(q)
+    assert rel_l2(out[0], out[1]) <= TOL_RUN
 
 
 def test_solver_steps_compose():
