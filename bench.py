@@ -433,6 +433,107 @@ def bench_order_sweep(sdg, args):
     return out
 
 
+def bench_operators(sdg, args, peaks, reps=30):
+    """The reference's standalone operator entry points on device arrays over
+    the bench box's elements (Ne^3 blocks of Nq^3 values, inputs larger than
+    L2): tensorprod_divlike_dirXYZ (OPT1 and GENERAL orders), gradlike,
+    divlike_var5 (5 variables a node), element matvec, Lift_hexahedral,
+    update_halo and the device mesh build.  Each is queued `reps` times on one
+    stream and timed on the host with a synchronize on both sides (calls of
+    0.1-3 ms, so the launch cost is a few per cent at most).  Bytes are the
+    arrays each call must read and write once (FP64), flops its
+    multiply-adds x 2."""
+    lib, A = sdg.lib, sdg.DeviceArray
+    p, ne = args.p, args.ne
+    nq, np_ = p + 1, (p + 1) ** 3
+    ne3 = ne ** 3
+    n = np_ * ne3
+    ntf = 6 * nq * nq
+    nhalo = 6 * ne * ne
+    nhn = nq * nq * nhalo
+    rng = np.random.default_rng(args.seed + 5)
+    x1, D, Dt, L = sdg.operator_generate(p)
+    Dd, Dtd, Ld = A(D), A(Dt), A(L)
+    hbm = measured_peaks()[0]
+    dfma = peaks["dfma_tflops"] if peaks else None
+
+    def timed(fn, k=reps):
+        fn()
+        sdg.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            fn()
+        sdg.synchronize()
+        return (time.perf_counter() - t0) / k
+
+    out = {"workload": f"{ne}^3 elements of order {p} ({n} nodes a field), device arrays, "
+                       f"{reps} queued calls each, host-timed with a synchronize on both sides",
+           "operators": {}}
+
+    def record(name, fn, nbytes, flops, ref):
+        t = timed(fn)
+        row = {"ms_per_call": t * 1e3, "gbs": nbytes / t / 1e9, "hbm_frac": nbytes / t / 1e9 / hbm,
+               "bytes_per_call": nbytes, "ref": ref}
+        if flops:
+            row["gflops"] = flops / t / 1e9
+            if dfma:
+                row["fp64_pipe_frac"] = flops / t / 1e12 / dfma
+        out["operators"][name] = row
+
+    fin = [A(rng.standard_normal(n)) for _ in range(3)]
+    fout = [A(n=n) for _ in range(3)]
+    chk = sdg._check
+    for opt, oname in ((sdg.OPT_OPT1, "OPT1"), (sdg.OPT_GENERAL, "GENERAL")):
+        record(f"tensorprod_divlike_dirXYZ ({oname})",
+               lambda opt=opt: chk(lib.sdg_tensorprod_divlike_dirXYZ_dev(
+                   fout[0].ptr, fout[1].ptr, fout[2].ptr, Dd.ptr, Dtd.ptr, fin[0].ptr,
+                   fin[1].ptr, fin[2].ptr, nq, ne3, opt, None), "divlike"),
+               48 * n, 6 * nq * n, "mod_dg_optr_kernel.f90:62-136")
+    record("tensorprod_gradlike_dirXYZ",
+           lambda: chk(lib.sdg_tensorprod_gradlike_dirXYZ_dev(
+               fout[0].ptr, fout[1].ptr, fout[2].ptr, Dd.ptr, Dtd.ptr, fin[0].ptr, nq, ne3,
+               None), "gradlike"),
+           32 * n, 6 * nq * n, "opt1 erb:166-219")
+    record("element_matvec_dir (z)",
+           lambda: chk(lib.sdg_element_matvec_dir_dev(3, fout[0].ptr, Dtd.ptr, fin[0].ptr, nq,
+                                                      ne3, None), "matvec"),
+           16 * n, 2 * nq * n, "opt1 erb:51-129")
+    lin = A(rng.standard_normal(ntf * ne3))
+    record("tensorprod_Lift_hexahedral",
+           lambda: chk(lib.sdg_tensorprod_Lift_hexahedral_dev(fout[0].ptr, Ld.ptr, lin.ptr, nq,
+                                                              ne3, None), "lift"),
+           8 * (n + ntf * ne3), 12 * n, "mod_dg_optr_kernel.f90:139-190")
+    del fin, fout, lin
+    # five variables a node: 3 inputs and 3 outputs of 5 n values
+    ne5 = max(1, ne3 // 5)
+    n5 = 5 * np_ * ne5
+    vin = [A(rng.standard_normal(n5)) for _ in range(3)]
+    vout = [A(n=n5) for _ in range(3)]
+    record("tensorprod_divlike_dirXYZ_var5",
+           lambda: chk(lib.sdg_tensorprod_divlike_dirXYZ_var5_dev(
+               vout[0].ptr, vout[1].ptr, vout[2].ptr, Dd.ptr, Dtd.ptr, vin[0].ptr, vin[1].ptr,
+               vin[2].ptr, nq, ne5, None), "var5"),
+           48 * n5, 6 * nq * n5, "opt1 erb:347-465")
+    out["operators"]["tensorprod_divlike_dirXYZ_var5"]["elements"] = ne5
+    del vin, vout
+    vm, vp = A(n=ntf * ne3, dtype=np.int32), A(n=ntf * ne3, dtype=np.int32)
+    nf, fs = A(n=3 * ntf * ne3), A(n=ntf * ne3)
+    es, hm = A(n=3 * n), A(n=nhn, dtype=np.int32)
+    record("mesh_setup (device)",
+           lambda: chk(lib.sdg_mesh_setup_dev(ne, ne, ne, p, 1.0, 1.0, 1.0, None, vm.ptr, vp.ptr,
+                                              nf.ptr, es.ptr, fs.ptr, None, hm.ptr, None),
+                       "mesh_setup"),
+           # VMapM, VMapP (4 B), normal_fn (24 B), Fscale (8 B) a face node, Escale 24 B a
+           # node, the halo map 4 B a halo node: written once
+           40 * ntf * ne3 + 24 * n + 4 * nhn, 0, "mod_mesh.f90:74-193")
+    f = A(n=np_ * (ne3 + nhalo))
+    record("update_halo",
+           lambda: chk(lib.sdg_update_halo_dev(f.ptr, hm.ptr, np_, ne3, nhn, None), "halo"),
+           20 * nhn, 0, "mod_mesh.f90:209-221")
+    out["operators"]["update_halo"]["halo_nodes"] = nhn
+    return out
+
+
 def bench_dropin(sdg, args, wl, fused_rate, opt=None):
     """The reference-shaped per-stage path on the bench workload, all on device
     arrays: mesh arrays built on the device (sdg_mesh_setup_dev), then per step
@@ -732,6 +833,8 @@ def run_ours(args, ws, rank, local):
     if ws == 1 and not args.no_dropin:
         line["dropin"] = bench_dropin(sdg, args, wl, value)
         line["dropin_evenodd"] = bench_dropin(sdg, args, wl, value, sdg.OPT_EVENODD)
+    if ws == 1 and not args.no_operators:
+        line["operators"] = bench_operators(sdg, args, peaks)
     if ws == 1 and not args.no_ensemble:
         line["ensemble"] = bench_ensemble(sdg, args)
     if ws == 1 and not args.no_serving:
@@ -777,6 +880,9 @@ def main() -> int:
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-dropin", action="store_true",
                     help="skip the per-stage drop-in path measurement")
+    ap.add_argument("--no-operators", action="store_true",
+                    help="skip the standalone operator entry points (divlike, gradlike, "
+                         "var5, matvec, Lift, update_halo, mesh build)")
     ap.add_argument("--batch-opt", choices=["auto", "general", "evenodd"], default="auto",
                     help="stage body of the batched kernels (ensemble and serving): auto = "
                          "chosen per order (the ensemble's tuner, the server's measured "
