@@ -450,11 +450,15 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
 // up to p = 12 the registers are capped at 32 for 64 warps (measured 1.0-1.16x
 // the three-block build, 100 against 91.5 GDOF-updates/s at p = 7); above
 // that shared memory admits three blocks and the cap would only spill.
-// FP64: four blocks of 256 threads (registers capped at 64): a block in its
-// load or flux phase leaves three others feeding the FP64 pipe.
+// FP64: four or five blocks of 256 threads (registers capped at 64 or 48): a
+// block in its load or flux phase leaves the others feeding the FP64 pipe.
+// Five measured faster on GB300 at most orders once stages 2-3 read the face
+// factors (1.02-1.06x up to p = 4, 1.005-1.013x at p = 6 and 8..13, 48
+// registers with small spills) and four at p = 5, 7, 14 and 15 (by 0.2-1.1 %).
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_min_blocks() {
-  return sizeof(CT) == 8 ? 4 : (P <= 3 || P == 5 || eo_lines<P, CT>() == 128) ? 8 : P <= 12 ? 4 : 3;
+  if (sizeof(CT) == 8) return (P == 5 || P == 7 || P >= 14) ? 4 : 5;
+  return (P <= 3 || P == 5 || eo_lines<P, CT>() == 128) ? 8 : P <= 12 ? 4 : 3;
 }
 
 // FP32 single-box kernel: F_y / F_z formed on the fly (FLY) at the orders
