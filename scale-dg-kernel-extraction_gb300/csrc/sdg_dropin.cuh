@@ -415,15 +415,27 @@ __global__ void __launch_bounds__(DropCfg<P>::THREADS) gradlike_kernel(const Div
   const long long g0 = eb * NP;
   for (int t = threadIdx.x; t < nloc * NP; t += T) f[t] = a.ix[g0 + t];
   __syncthreads();
-  for (int t = threadIdx.x; t < nloc * NP; t += T) {
-    const int le = t / NP;
-    const int n = t - le * NP;
-    const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
-    const double* fe = f + le * NP;
-    if (a.ox) a.ox[g0 + t] = line_sum<NQ, false, NQ>(sD + i, fe + j * NQ + k * NQ2, 1);
-    if (a.oy) a.oy[g0 + t] = line_sum<NQ, false, 1>(sDt + j * NQ, fe + i + k * NQ2, NQ);
-    if (a.oz) a.oz[g0 + t] = line_sum<NQ, false, 1>(sDt + k * NQ, fe + i + j * NQ, NQ2);
-  }
+  // one direction at a time: a thread keeps one running sum live, not three
+  // (82 registers and three blocks an SM at p = 7 when the three were
+  // interleaved)
+  if (a.ox)
+    for (int t = threadIdx.x; t < nloc * NP; t += T) {
+      const int le = t / NP, n = t - le * NP;
+      const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
+      a.ox[g0 + t] = line_sum<NQ, false, NQ>(sD + i, f + le * NP + j * NQ + k * NQ2, 1);
+    }
+  if (a.oy)
+    for (int t = threadIdx.x; t < nloc * NP; t += T) {
+      const int le = t / NP, n = t - le * NP;
+      const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
+      a.oy[g0 + t] = line_sum<NQ, false, 1>(sDt + j * NQ, f + le * NP + i + k * NQ2, NQ);
+    }
+  if (a.oz)
+    for (int t = threadIdx.x; t < nloc * NP; t += T) {
+      const int le = t / NP, n = t - le * NP;
+      const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
+      a.oz[g0 + t] = line_sum<NQ, false, 1>(sDt + k * NQ, f + le * NP + i + j * NQ, NQ2);
+    }
 }
 
 template <int P>
