@@ -77,7 +77,8 @@ struct StageArgs {
   // face node of each element (2*Nfp*6 doubles an element).  A stage with
   // fc_out forms them from u, v, w and stores them; a stage with fc_in reads
   // them instead (same bits), so the three stages of one RK step, which share
-  // the velocity, form them once.  Both null: formed inline.
+  // the velocity (main.f90:58-67 passes the same u, v, w to the three
+  // advect3d_eq_cal_tend calls), form them once.  Both null: formed inline.
   double* fc_out;
   const double* fc_in;
 };
