@@ -1,9 +1,10 @@
 """Benchmark of the 3D DG advection hot path on one GB300 (or N replicas).
 
 Workload: the periodic unit box, Ne = 32^3 hexahedra of order p = 7
-(512 nodes each, 16.8M DOF), seeded Gaussian tracer (sigma 0.1) in a seeded
-smooth velocity field, SSP-RK3 with dt at CFL 0.1, FP64 plain form.  One
-"step" is one SSP-RK3 time step of the whole box (three fused stage kernels).
+(512 nodes each, 16.8M DOF), the reference's own operators
+(operator_data/p7.dat), seeded Gaussian tracer (sigma 0.1) in a seeded smooth
+velocity field, SSP-RK3 with dt at CFL 0.1, FP64 plain form.  One "step" is
+one SSP-RK3 time step of the whole box (three fused stage kernels).
 
 Metric: GDOF-updates/s = Np * Ne * 3 * steps / t / 1e9 (one DOF-update is one
 DOF advanced through one RK stage).  `value` is timed with CUDA events on the
@@ -11,12 +12,22 @@ solver's stream with the state resident in HBM; `e2e` goes through the C ABI
 with pinned host buffers (upload q,u,v,w, one step, download q, every step).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--results FILE]
+
+Output: the secondary measurements (emulated FP64, the per-stage drop-in
+path, standalone operators, the batched ensemble, serving, the order sweep)
+are printed first, one JSON line each with a "section" key; the LAST line is
+the compact headline (metric, value, e2e, roofline, cpu_baseline, clocks,
+parity and a serving / ensemble summary).  --results also writes every line
+to one JSON file.
 
 With --impl reference the CPU oracle (a C + OpenMP restatement of the
 reference's Fortran path, which has no Fortran compiler to build it with) is
-timed on the host cores on the same workload.  Under torchrun with N > 1 every
-rank runs an independent replica (the path is built for one GPU and exchanges
-nothing between boxes); rank 0 prints.
+timed on the host cores on the same workload, through its timing build
+(-O3 -fopenmp, multiply-add contraction, -mcpu=native on aarch64); that arm
+loads only the oracle.  Under torchrun with N > 1 every rank runs an
+independent replica (the path is built for one GPU and exchanges nothing
+between boxes); rank 0 prints.
 """
 from __future__ import annotations
 
@@ -132,9 +143,11 @@ def dist_env():
 
 
 def make_workload(p: int, ne: int, seed: int):
-    import sdg
+    """The bench box on the reference's own operators (operator_data/p{p}.dat,
+    the committed bit-exact fixture); numpy only, so that the reference arm
+    loads nothing of the product."""
     import workloads as W
-    x, D, Dt, L = sdg.operator_generate(p)
+    x, D, Dt, L = W.reference_operators(p)
     q, u, v, w = W.blob(ne, ne, ne, x, seed)
     dt = W.cfl_dt(ne, ne, ne, p, u, v, w)
     return dict(x=x, D=D, Dt=Dt, L=L, q=q, u=u, v=v, w=w, dt=dt)
@@ -166,15 +179,17 @@ class OracleBox:
                                self.O.OPT1)[: m.Np * m.Ne]
 
     def time_steps(self, min_seconds: float, max_steps: int, warmup: int = 0):
-        """Steps a copy of the state; returns (steps, seconds)."""
+        """Steps a copy of the state in the reference's OPT1 order through the
+        oracle's timing build (contraction allowed, -mcpu=native on aarch64,
+        all host cores); returns (steps, seconds)."""
         O, wl, m = self.O, self.wl, self.m
         q = self.arrs[0].copy()
         args = (self.arrs[1], self.arrs[2], self.arrs[3], wl["D"], wl["Dt"], wl["L"], wl["dt"])
         for _ in range(warmup):
-            O.run(m, q, *args[:3], *args[3:6], args[6], 1, O.OPT1)
+            O.run(m, q, *args[:3], *args[3:6], args[6], 1, O.OPT1, fast=True)
         steps, t0 = 0, time.perf_counter()
         while steps < max_steps:
-            O.run(m, q, *args[:3], *args[3:6], args[6], 1, O.OPT1)
+            O.run(m, q, *args[:3], *args[3:6], args[6], 1, O.OPT1, fast=True)
             steps += 1
             if time.perf_counter() - t0 >= min_seconds:
                 break
@@ -208,11 +223,11 @@ def run_reference(args, ws, rank):
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Gaussian tracer, seeded smooth velocity)",
-        "config": config(args),
+        "config": config(args, reference=True),
         "cpu_baseline": {"value": v, "unit": "GDOF-updates/s", "cores": threads, "kind": "port",
-                         "sample": f"{steps} SSP-RK3 steps of the full {args.ne}^3 p={args.p} box "
-                                   "(C + OpenMP restatement of the Fortran reference; "
-                                   "the reference itself has no compiler here)"},
+                         "sample": f"{steps} SSP-RK3 steps of the full {args.ne}^3 p={args.p} box, "
+                                   "OPT1 order (C + OpenMP restatement of the Fortran reference, "
+                                   "timing build; no Fortran compiler for the reference itself)"},
         "e2e": {"value": v, "unit": "GDOF-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -228,13 +243,17 @@ def metric_name(args) -> str:
     return f"GDOF-updates/s (p={args.p}, {args.ne}^3, {PREC_LABEL[args.precision]})"
 
 
-def config(args) -> dict:
+def config(args, reference: bool = False) -> dict:
+    """The workload's description.  The reference arm times the reference's
+    OPT1 order; ours names the order its stage kernel sums in."""
     ndof = (args.p + 1) ** 3 * args.ne ** 3
     ws_bytes = ndof * (8 * 3 + (12 if args.precision == "fp32" else 24))
     return {"workload": f"3D DG advection, periodic unit box, Ne={args.ne}^3, p={args.p}, "
                         f"SSP-RK3, CFL 0.1, {args.precision} plain form",
-            "p": args.p, "Ne": [args.ne] * 3, "dof": ndof, "opt": args.opt.upper(),
-            "precision": args.precision,
+            "p": args.p, "Ne": [args.ne] * 3, "dof": ndof,
+            "opt": "OPT1" if reference else args.opt.upper(),
+            "precision": "fp64" if reference else args.precision,
+            "operators": f"operator_data/p{args.p}.dat (the reference's file, bit for bit)",
             "l2": f"inputs larger than L2 (state+velocity working set {ws_bytes / 1e6:.0f} MB "
                   "vs 129 MB L2)",
             "parallelism": "replicas (one independent box per GPU)"}
@@ -264,9 +283,25 @@ def time_solver(sdg, wl, p, ne, prec, steps, warmup, local, barrier, sample_cloc
 
 
 def roofline(precision, p, ne, ndof, t, steps, peaks, opt="opt1"):
+    """The stage kernel against its roofs.
+
+    HBM: achieved = the algorithmic bytes per DOF-update (45.33 B FP64 and
+    emulated, 33.33 B FP32: state, velocity and the RK buffers) x the DOF of
+    one launch / the average launch time (3 launches a step, nothing else in
+    the step).  The face-flux velocity factors the even-odd FP64 and emulated
+    stages share within a step are implementation bytes, reported beside it
+    (`implementation_bytes_per_dof_update`) and not counted.  `traffic` is
+    the ncu DRAM bytes per launch of the same kernel.
+
+    Compute: the FP64 pipe binds the FP64 forms (1.2 TFLOP/s DFMA against
+    88.75 flops a DOF-update at p = 7).  `compute.frac` is that pipe's busy
+    share from the kernel's ncu capture (sm__pipe_fp64_cycles_active);
+    `achieved_tflops` counts the reference's formulas (25 + 6 Nq + 126 / Nq
+    flops a DOF-update) against the DFMA peak measured live."""
     launches = 3 * steps
     avg_launch = t / launches
-    bpd = BYTES_PER_DOF_UPDATE[precision] + face_factor_bytes(precision, opt, p)
+    bpd = BYTES_PER_DOF_UPDATE[precision]
+    impl = face_factor_bytes(precision, opt, p)
     achieved = bpd * ndof / avg_launch / 1e9
     peak, peak_kind = measured_peaks()
     per_gpu = ndof * 3 * steps / t / 1e9
@@ -276,7 +311,7 @@ def roofline(precision, p, ne, ndof, t, steps, peaks, opt="opt1"):
               "fp64emu": f"stage_emu_kernel<{p}>"}[precision]
     tkey = f"stage_{precision}_p{p}_ne{ne}"
     if precision == "fp64" and opt == "evenodd":
-        kernel, tkey = f"stage_eo_kernel<{p}>", f"stage_fp64eo_p{p}_ne{ne}"
+        kernel, tkey = f"stage_eo_kernel<{p},double>", f"stage_fp64eo_p{p}_ne{ne}"
     elif precision == "fp64emu" and opt == "evenodd":
         kernel, tkey = f"stage_emu_eo_kernel<{p}>", f"stage_fp64emueo_p{p}_ne{ne}"
     elif precision == "fp32" and opt == "evenodd":
@@ -285,26 +320,25 @@ def roofline(precision, p, ne, ndof, t, steps, peaks, opt="opt1"):
             "frac": achieved / peak,
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
             "algorithmic_bytes_per_dof_update": bpd,
+            "implementation_bytes_per_dof_update": impl,
             "traffic": load_traffic(tkey),
             "kernel": kernel, "avg_launch_ms": avg_launch * 1e3}
     if peaks is not None:
-        roof["compute"] = {
-            "pipe": "FP64 (DFMA)" if precision == "fp64" else "FP32 (FFMA)",
-            "flops_per_dof_update": fl,
-            "achieved_tflops": fl * per_gpu / 1e3,
-            "peak_tflops_measured_live": peaks[pipe],
-            "frac": fl * per_gpu / 1e3 / peaks[pipe],
-            "note": ("algorithmic FP64 flops; the emulated path spends ~20 FP32 ops per "
-                     "FP64 flop" if precision == "fp64emu" else
-                     "algorithmic flops of the reference's formulas; the even-odd body "
-                     "issues about 30 % fewer FP64 operations, so this fraction can pass 1"
-                     if opt == "evenodd" else "algorithmic flops")}
-        if precision == "fp64":
-            roof["binding_roof"] = "fp64_pipe" if roof["compute"]["frac"] > roof["frac"] else "hbm"
+        comp = {"pipe": "FP64 (DFMA)" if precision == "fp64" else "FP32 (FFMA)",
+                "flops_per_dof_update": fl,
+                "achieved_tflops": fl * per_gpu / 1e3,
+                "peak_tflops_measured_live": peaks[pipe]}
         busy = load_traffic(tkey, "fp64_pipe_active")
-        if busy is not None:
-            # sm__pipe_fp64_cycles_active of the same kernel's ncu capture
-            roof["compute"]["fp64_pipe_active_ncu"] = busy
+        if busy is not None and precision in ("fp64", "fp64emu"):
+            comp["frac"] = busy
+            comp["frac_source"] = "sm__pipe_fp64_cycles_active, ncu capture of this kernel"
+        else:
+            comp["frac"] = fl * per_gpu / 1e3 / peaks[pipe]
+            comp["frac_source"] = "reference-formula flops / live peak"
+        roof["compute"] = comp
+        if precision == "fp64":
+            # the FP64 pipe binds when it is busier than HBM
+            roof["binding_roof"] = "fp64_pipe" if comp["frac"] > roof["frac"] else "hbm"
     return roof
 
 
@@ -336,7 +370,7 @@ def ensemble_workload(n, seed):
 def bench_ensemble(sdg, args):
     import workloads as W
     members = ensemble_workload(args.ens_n, args.seed + 1000)
-    ops = {p: sdg.operator_generate(p) for p in (3, 5, 7)}
+    ops = {p: W.reference_operators(p) for p in (3, 5, 7)}
     t0 = time.perf_counter()
     ens = sdg.Ensemble([m["dims"] for m in members], [m["p"] for m in members],
                        [m["dt"] for m in members], ops)
@@ -405,7 +439,7 @@ def bench_order_sweep(sdg, args):
     out = []
     for p in range(1, 16):
         ne = int(round(256.0 / (p + 1)))
-        x, D, Dt, L = sdg.operator_generate(p)
+        x, D, Dt, L = W.reference_operators(p)
         q, u, v, w = W.blob(ne, ne, ne, x, args.seed + p)
         dt = W.cfl_dt(ne, ne, ne, p, u, v, w)
         ndof = q.size
@@ -452,7 +486,8 @@ def bench_operators(sdg, args, peaks, reps=30):
     nhalo = 6 * ne * ne
     nhn = nq * nq * nhalo
     rng = np.random.default_rng(args.seed + 5)
-    x1, D, Dt, L = sdg.operator_generate(p)
+    import workloads as W
+    x1, D, Dt, L = W.reference_operators(p)
     Dd, Dtd, Ld = A(D), A(Dt), A(L)
     hbm = measured_peaks()[0]
     dfma = peaks["dfma_tflops"] if peaks else None
@@ -615,7 +650,7 @@ def bench_serving(sdg, args, rate=None, plain_cache=None):
     the plain-path time of its sample across calls."""
     import math
     import workloads as W
-    ops = {p: sdg.operator_generate(p) for p in range(2, 12)}
+    ops = {p: W.reference_operators(p) for p in range(2, 12)}
     rng = W.SplitMix64(args.seed + 5000)
     reqs, arrivals, t = [], [], 0.0
     for i in range(args.serve_n):
@@ -724,6 +759,63 @@ def whole_job_rate(ws: int, ndof: int, steps: int, t_max: float) -> float:
     return ws * ndof * 3 * steps / t_max / 1e9
 
 
+def _round(x, sig=4):
+    """Rounds every float of a JSON-able structure to `sig` significant digits."""
+    if isinstance(x, float):
+        return float(f"{x:.{sig}g}")
+    if isinstance(x, dict):
+        return {k: _round(v, sig) for k, v in x.items()}
+    if isinstance(x, list):
+        return [_round(v, sig) for v in x]
+    return x
+
+
+def headline_line(args, ws, value, t, roof, cpu, e2e, clk, parity, sections) -> dict:
+    """The compact last line (kept well under 2 KB): the contract's keys, the
+    roofline, the CPU baseline, e2e, clocks and parity, plus one-line
+    summaries of serving (solves/s and p99 against the plain GPU path) and of
+    the batched ensemble.  Everything else is in the earlier section lines."""
+    line = {
+        "metric": metric_name(args), "value": value, "unit": "GDOF-updates/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp64": "f64", "fp64emu": "f64-state/double-float",
+                  "fp32": "f32-compute/f64-state"}[args.precision],
+        "data": "synthetic (seeded Gaussian tracer, seeded smooth velocity)",
+        "config": config(args),
+        "roofline": {k: roof[k] for k in ("bound", "achieved", "peak", "unit", "frac", "traffic",
+                                          "algorithmic_bytes_per_dof_update",
+                                          "implementation_bytes_per_dof_update", "kernel",
+                                          "binding_roof") if k in roof},
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * args.steps, "clocks": clk,
+        "parity": parity,
+    }
+    if "compute" in roof:
+        c = roof["compute"]
+        line["roofline"]["compute"] = {k: c[k] for k in ("pipe", "frac", "frac_source",
+                                                         "achieved_tflops",
+                                                         "peak_tflops_measured_live")}
+    if e2e is not None:
+        line["e2e"] = {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step",
+                                           "d2h_bytes_per_step", "steps")}
+    srv = sections.get("serving_saturated") or sections.get("serving")
+    if srv:
+        line["serving"] = {k: srv[k] for k in ("offered_rate_req_s", "solves_per_s",
+                                               "p50_latency_s", "p99_latency_s",
+                                               "ratio_vs_plain")}
+    ens = sections.get("ensemble")
+    if ens:
+        line["ensemble"] = {k: ens[k] for k in ("solves_per_s", "ratio_vs_plain",
+                                                "rel_l2_vs_fp64_max", "hbm_frac")}
+    return _round(line)
+
+
+def emit_section(name: str, body, out: dict) -> None:
+    """Prints one secondary measurement as its own JSON line and keeps it."""
+    out[name] = body
+    print(json.dumps({"section": name, "result": body}), flush=True)
+
+
 def run_ours(args, ws, rank, local):
     import sdg
     if sdg.device_count() < 1:
@@ -776,6 +868,7 @@ def run_ours(args, ws, rank, local):
 
     # ---- the other FP64-state path on the same workload ----
     other = None
+    tend_emu = None
     if args.precision == "fp64" and not args.no_emu:
         se, te_, _ = time_solver(sdg, wl, p, ne, PRECISIONS["fp64emu"], args.steps,
                                  args.warmup, local, barrier, False, OPTS[args.opt])
@@ -786,7 +879,6 @@ def run_ours(args, ws, rank, local):
                  "value": ws * ndof * 3 * args.steps / te_ / 1e9, "unit": "GDOF-updates/s",
                  "ms_per_step": 1e3 * te_ / args.steps,
                  "roofline": roofline("fp64emu", p, ne, ndof, te_, args.steps, peaks, args.opt)}
-        tend_emu = None
         if rank == 0 and not args.no_cpu_baseline:
             se.upload(wl["q"], wl["u"], wl["v"], wl["w"])
             tend_emu = se.tendency()
@@ -796,6 +888,10 @@ def run_ours(args, ws, rank, local):
         rep.close()
         return 0
 
+    sections: dict = {}
+    if e2e is not None:
+        emit_section("e2e_detail", e2e, sections)
+    emit_section("roofline_detail", roof, sections)
     cpu = None
     parity = None
     if not args.no_cpu_baseline:
@@ -805,54 +901,49 @@ def run_ours(args, ws, rank, local):
         def rl2(x):
             return float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
 
-        parity = {"tendency_rel_l2_vs_oracle": {args.precision: rl2(tend_main)},
+        parity = {"tendency_rel_l2_vs_oracle": rl2(tend_main),
                   "tolerance": 1e-12 if args.precision != "fp32" else 1e-5,
-                  "state": "initial state of the bench workload"}
+                  "state": "initial state, reference operators p%d.dat" % p}
         if other is not None:
-            parity["tendency_rel_l2_vs_oracle"]["fp64emu"] = rl2(tend_emu)
             other["tendency_rel_l2_vs_fp64_oracle"] = rl2(tend_emu)
         if ws == 1:
             steps, secs = ob.time_steps(args.cpu_seconds, 10 ** 6)
             cpu = {"value": ndof * 3 * steps / secs / 1e9, "unit": "GDOF-updates/s",
                    "cores": ob.threads, "kind": "port",
-                   "sample": f"{steps} SSP-RK3 steps of the same {ne}^3 p={p} box in FP64 "
-                             f"({secs:.1f} s; C + OpenMP restatement of the Fortran "
-                             "reference)"}
-    line = {
-        "metric": metric_name(args), "value": value, "unit": "GDOF-updates/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp64": "f64", "fp64emu": "f64-state/double-float",
-                  "fp32": "f32-compute/f64-state"}[args.precision],
-        "data": "synthetic (seeded Gaussian tracer, seeded smooth velocity)",
-        "config": config(args), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": 3 * args.steps, "clocks": clk, "parity": parity,
-    }
+                   "sample": f"{steps} SSP-RK3 steps of the same {ne}^3 p={p} box, OPT1 "
+                             f"order ({secs:.1f} s; C + OpenMP restatement of the Fortran "
+                             "reference, timing build)"}
     if other is not None:
-        line["fp64_emulated"] = other
+        emit_section("fp64_emulated", other, sections)
     if ws == 1 and not args.no_dropin:
-        line["dropin"] = bench_dropin(sdg, args, wl, value)
-        line["dropin_evenodd"] = bench_dropin(sdg, args, wl, value, sdg.OPT_EVENODD)
+        emit_section("dropin", bench_dropin(sdg, args, wl, value), sections)
+        emit_section("dropin_evenodd", bench_dropin(sdg, args, wl, value, sdg.OPT_EVENODD),
+                     sections)
     if ws == 1 and not args.no_operators:
-        line["operators"] = bench_operators(sdg, args, peaks)
+        emit_section("operators", bench_operators(sdg, args, peaks), sections)
     if ws == 1 and not args.no_ensemble:
-        line["ensemble"] = bench_ensemble(sdg, args)
+        emit_section("ensemble", bench_ensemble(sdg, args), sections)
     if ws == 1 and not args.no_serving:
         plain_cache = {}
-        line["serving"] = bench_serving(sdg, args, plain_cache=plain_cache)
+        emit_section("serving", bench_serving(sdg, args, plain_cache=plain_cache), sections)
         # the same request stream offered faster than the GPU can serve it:
         # throughput and tail latency of the saturated server
-        line["serving_saturated"] = bench_serving(sdg, args, args.serve_rate_saturated,
-                                                  plain_cache)
+        emit_section("serving_saturated",
+                     bench_serving(sdg, args, args.serve_rate_saturated, plain_cache), sections)
         # the offered rate swept across the 10-2000 req/s range
-        line["serving_rate_sweep"] = []
+        sweep = []
         for r in (float(x) for x in args.serve_sweep.split(",") if x):
             res = bench_serving(sdg, args, r, plain_cache)
-            line["serving_rate_sweep"].append(
-                {k: res[k] for k in ("offered_rate_req_s", "solves_per_s", "p50_latency_s",
-                                     "p99_latency_s", "gdof_updates_per_s", "ratio_vs_plain")})
+            sweep.append({k: res[k] for k in ("offered_rate_req_s", "solves_per_s",
+                                              "p50_latency_s", "p99_latency_s",
+                                              "gdof_updates_per_s", "ratio_vs_plain")})
+        emit_section("serving_rate_sweep", sweep, sections)
     if ws == 1 and not args.no_sweep:
-        line["order_sweep"] = bench_order_sweep(sdg, args)
+        emit_section("order_sweep", bench_order_sweep(sdg, args), sections)
+    line = headline_line(args, ws, value, t, roof, cpu, e2e, clk, parity, sections)
+    if args.results:
+        with open(args.results, "w") as f:
+            json.dump({"headline": line, "sections": sections}, f, indent=1)
     print(json.dumps(line), flush=True)
     rep.close()
     return 0
@@ -905,6 +996,8 @@ def main() -> int:
     ap.add_argument("--serve-plain-sample", type=int, default=8)
     ap.add_argument("--no-microbench", action="store_true",
                     help="skip the live DFMA/FFMA peak measurement")
+    ap.add_argument("--results", default=None,
+                    help="also write the headline and every section to this JSON file")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

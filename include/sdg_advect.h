@@ -485,6 +485,13 @@ int sdg_server_submit(sdg_server* s, const sdg_request* r, double* out_state,
 int sdg_server_wait(sdg_server* s, uint64_t ticket, double timeout_s,
                     sdg_result* res);
 int sdg_server_get_stats(sdg_server* s, sdg_server_stats* out);
+/* Host-side fault injection for tests of the failure path: the next rebuild
+ * of the active set's device tables after a request completes reports
+ * SDG_ERR_OUT_OF_MEMORY as a failed allocation would.  The server then
+ * finishes every active request with that status, records it as
+ * fatal_status and launches nothing more for them.  No device fault is
+ * involved.  No reference counterpart. */
+int sdg_server_inject_rebuild_failure(sdg_server* s);
 int sdg_server_reset_stats(sdg_server* s);
 int sdg_server_destroy(sdg_server* s);
 

@@ -16,6 +16,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libsdg_oracle.so")
+# the same source built for timing (multiply-add contraction, -mcpu=native on
+# aarch64); only the timed CPU baseline loads it, never a parity check
+FAST_LIB_PATH = os.path.join(HERE, "_build", "libsdg_oracle_fast.so")
 
 GENERAL = 1
 OPT1 = 2
@@ -23,49 +26,65 @@ OPT1 = 2
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _lib = None
+_fast_lib = None
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (gcc, a second or two)."""
-    if force or not os.path.exists(LIB_PATH) or (
-        os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "sdg_oracle.c"))
-    ):
-        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    """Compile both oracle builds with the Makefile (gcc, a few seconds)."""
+    src = max(os.path.getmtime(os.path.join(HERE, f)) for f in
+              ("sdg_oracle.c", "sdg_oracle.h", "Makefile"))
+    if force or any(not os.path.exists(p) or os.path.getmtime(p) < src
+                    for p in (LIB_PATH, FAST_LIB_PATH)):
+        subprocess.run(["make", "-s", "-C", HERE] + (["-B"] if force else []), check=True)
     return LIB_PATH
 
 
 def lib():
+    """The parity build (no multiply-add contraction)."""
     global _lib
     if _lib is None:
         build()
-        L = C.CDLL(LIB_PATH)
-        i = C.c_int
-        d = C.c_double
-        L.sdgo_read_operator_file.argtypes = [C.c_char_p, i, _dp, _dp, _dp, _dp]
-        L.sdgo_read_operator_file.restype = i
-        L.sdgo_fmask.argtypes = [i, _ip]
-        L.sdgo_nhalo.argtypes = [i, i, i]
-        L.sdgo_nhalo.restype = i
-        L.sdgo_mesh_setup.argtypes = [i, i, i, i, d, d, d, _dp, _ip, _ip, _dp, _dp, _dp, _dp, _ip]
-        L.sdgo_update_halo.argtypes = [_dp, _ip, i, i, i]
-        L.sdgo_cal_elembnd_flux.argtypes = [_dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp, _dp, i, i, i, i]
-        L.sdgo_divlike.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, i, i]
-        L.sdgo_lift.argtypes = [_dp, _dp, _dp, i]
-        L.sdgo_gradlike.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, i]
-        L.sdgo_divlike_var5.argtypes = [_dp] * 8 + [i]
-        L.sdgo_cal_dqdt.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
-                                    i, i, i, i, i, i]
-        L.sdgo_cal_tend.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip,
-                                    _dp, _dp, _dp, i, i, i, i, i, i]
-        L.sdgo_cal_tend.restype = i
-        L.sdgo_rk_stage.argtypes = [_dp, _dp, _dp, i, i, i, d]
-        L.sdgo_run.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp,
-                               _dp, _dp, _ip, i, i, i, i, d, i, i, C.c_void_p]
-        L.sdgo_run.restype = i
-        L.sdgo_ic_sine.argtypes = [_dp, _dp, _dp, _dp, _dp, i, i, d, d, d]
-        L.sdgo_num_threads.restype = i
-        _lib = L
+        _lib = _declare(C.CDLL(LIB_PATH))
     return _lib
+
+
+def fast_lib():
+    """The timing build (contraction allowed): for the timed CPU baseline only."""
+    global _fast_lib
+    if _fast_lib is None:
+        build()
+        _fast_lib = _declare(C.CDLL(FAST_LIB_PATH))
+    return _fast_lib
+
+
+def _declare(L):
+    """Declares the argument types of the exported functions on a loaded build."""
+    i = C.c_int
+    d = C.c_double
+    L.sdgo_read_operator_file.argtypes = [C.c_char_p, i, _dp, _dp, _dp, _dp]
+    L.sdgo_read_operator_file.restype = i
+    L.sdgo_fmask.argtypes = [i, _ip]
+    L.sdgo_nhalo.argtypes = [i, i, i]
+    L.sdgo_nhalo.restype = i
+    L.sdgo_mesh_setup.argtypes = [i, i, i, i, d, d, d, _dp, _ip, _ip, _dp, _dp, _dp, _dp, _ip]
+    L.sdgo_update_halo.argtypes = [_dp, _ip, i, i, i]
+    L.sdgo_cal_elembnd_flux.argtypes = [_dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp, _dp, i, i, i, i]
+    L.sdgo_divlike.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, i, i]
+    L.sdgo_lift.argtypes = [_dp, _dp, _dp, i]
+    L.sdgo_gradlike.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, i]
+    L.sdgo_divlike_var5.argtypes = [_dp] * 8 + [i]
+    L.sdgo_cal_dqdt.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                i, i, i, i, i, i]
+    L.sdgo_cal_tend.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip,
+                                _dp, _dp, _dp, i, i, i, i, i, i]
+    L.sdgo_cal_tend.restype = i
+    L.sdgo_rk_stage.argtypes = [_dp, _dp, _dp, i, i, i, d]
+    L.sdgo_run.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp,
+                           _dp, _dp, _ip, i, i, i, i, d, i, i, C.c_void_p]
+    L.sdgo_run.restype = i
+    L.sdgo_ic_sine.argtypes = [_dp, _dp, _dp, _dp, _dp, i, i, d, d, d]
+    L.sdgo_num_threads.restype = i
+    return L
 
 
 def num_threads() -> int:
@@ -176,14 +195,15 @@ def lift(Lift, flux_e, Nq):
     return out
 
 
-def run(mesh: Mesh, q, u, v, w, D, Dt, Lift, dt, nstep, opt=OPT1, minmax=False):
+def run(mesh: Mesh, q, u, v, w, D, Dt, Lift, dt, nstep, opt=OPT1, minmax=False, fast=False):
     """Time loop of main.f90:51-80.  q is updated in place ((Np,NeA), owned
-    part meaningful).  Returns the per-step (min, max) array when asked."""
+    part meaningful).  Returns the per-step (min, max) array when asked.
+    fast=True runs the timing build (for the timed CPU baseline only)."""
     m = mesh
     q0 = np.zeros_like(q)
     dqdt = np.zeros_like(q)
     mm = np.zeros(2 * max(nstep, 1)) if minmax else None
-    st = lib().sdgo_run(q, q0, dqdt, u, v, w, D, Dt, Lift, m.VMapM, m.VMapP, m.normal_fn,
+    st = (fast_lib() if fast else lib()).sdgo_run(q, q0, dqdt, u, v, w, D, Dt, Lift, m.VMapM, m.VMapP, m.normal_fn,
                         m.Escale, m.Fscale, m.halo_src_map, m.Nq, m.Ne, m.NeA, m.NhaloNode,
                         float(dt), int(nstep), opt,
                         mm.ctypes.data_as(C.c_void_p) if mm is not None else None)

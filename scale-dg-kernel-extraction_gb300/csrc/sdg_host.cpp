@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -35,6 +36,33 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
                    : SDG_ERR_CUDA;
   return fail(st, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file,
               line);
+}
+
+int set_kernel_smem(const void* func, int smem, bool max_carveout) {
+  int dev = 0;
+  SDG_CUDA_TRY(cudaGetDevice(&dev));
+  struct Key {
+    const void* func;
+    int dev, smem;
+    bool carve;
+    bool operator==(const Key& o) const {
+      return func == o.func && dev == o.dev && smem == o.smem && carve == o.carve;
+    }
+  };
+  static std::mutex mu;
+  static std::vector<Key> done;  // a few dozen kernels at most
+  const Key k{func, dev, smem, max_carveout};
+  {
+    std::lock_guard<std::mutex> g(mu);
+    if (std::find(done.begin(), done.end(), k) != done.end()) return SDG_OK;
+  }
+  SDG_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  if (max_carveout)
+    SDG_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      (int)cudaSharedmemCarveoutMaxShared));
+  std::lock_guard<std::mutex> g(mu);
+  if (std::find(done.begin(), done.end(), k) == done.end()) done.push_back(k);
+  return SDG_OK;
 }
 
 int require_device() {

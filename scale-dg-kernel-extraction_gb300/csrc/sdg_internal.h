@@ -33,6 +33,13 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Raises a kernel's dynamic shared-memory limit to smem bytes (and, when
+// asked, prefers the largest shared-memory carveout) on the current device.
+// Kernel attributes are per device, so this records (kernel, device, smem)
+// and sets them once per device; it is safe to call from several host
+// threads at once.
+int set_kernel_smem(const void* func, int smem, bool max_carveout);
+
 // Checks the first CUDA device is usable; returns SDG_OK or an error status.
 int require_device();
 

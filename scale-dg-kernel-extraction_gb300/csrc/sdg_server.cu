@@ -79,6 +79,10 @@ struct sdg_server {
   Clock::time_point t_first_submit{}, t_last_done{};
   bool any_submit = false;
   int fatal = SDG_OK;
+  // host-side fault injection (sdg_server_inject_rebuild_failure): the next
+  // table rebuild after a completion reports an allocation failure
+  bool inject_on_completion = false;
+  bool inject_rebuild_failure = false;
 };
 
 namespace {
@@ -143,17 +147,27 @@ int rebuild_tables(sdg_server* s) {
     for (long long b = 0; b < I.box.Ne; b += e)
       items.push_back({i, (int)b, (int)std::min<long long>(e, I.box.Ne - b)});
   }
+  // grow a table only once its new allocation has succeeded, so that a
+  // failed allocation leaves the old table and its capacity consistent
+  if (s->inject_rebuild_failure) {
+    s->inject_rebuild_failure = false;
+    return fail(SDG_ERR_OUT_OF_MEMORY, "table rebuild failed (injected)");
+  }
   if (n > s->d_inst_cap) {
+    const int cap = std::max(n, 2 * s->d_inst_cap);
+    BatchInst* t = nullptr;
+    SDG_CUDA_TRY(cudaMalloc(&t, sizeof(BatchInst) * cap));
     cudaFree(s->d_inst);
-    s->d_inst = nullptr;
-    s->d_inst_cap = std::max(n, 2 * s->d_inst_cap);
-    SDG_CUDA_TRY(cudaMalloc(&s->d_inst, sizeof(BatchInst) * s->d_inst_cap));
+    s->d_inst = t;
+    s->d_inst_cap = cap;
   }
   if ((int)items.size() > s->d_items_cap) {
+    const int cap = std::max((int)items.size(), 2 * s->d_items_cap);
+    BatchItem* t = nullptr;
+    SDG_CUDA_TRY(cudaMalloc(&t, sizeof(BatchItem) * cap));
     cudaFree(s->d_items);
-    s->d_items = nullptr;
-    s->d_items_cap = std::max((int)items.size(), 2 * s->d_items_cap);
-    SDG_CUDA_TRY(cudaMalloc(&s->d_items, sizeof(BatchItem) * s->d_items_cap));
+    s->d_items = t;
+    s->d_items_cap = cap;
   }
   if (n)
     SDG_CUDA_TRY(cudaMemcpyAsync(s->d_inst, inst.data(), sizeof(BatchInst) * n,
@@ -185,6 +199,19 @@ void finish(sdg_server* s, Req* q, int status) {
     q->mem = nullptr;
     s->bytes_in_use -= q->bytes;
   }
+}
+
+// A failure that leaves the active set without usable tables (a failed step,
+// a failed table rebuild): every active request finishes with the status,
+// its memory goes back to the pool, and the server records the status.  The
+// scheduler then launches nothing until new requests are admitted.
+void fail_active(sdg_server* s, int st) {
+  s->fatal = st;
+  for (Req* q : s->active) finish(s, q, st);
+  s->active.clear();
+  s->n_items = 0;
+  s->groups.clear();
+  s->cv_done.notify_all();
 }
 
 void worker_loop(sdg_server* s) {
@@ -224,10 +251,7 @@ void worker_loop(sdg_server* s) {
     if (changed) {
       const int st = rebuild_tables(s);
       if (st != SDG_OK) {
-        s->fatal = st;
-        for (Req* q : s->active) finish(s, q, st);
-        s->active.clear();
-        s->cv_done.notify_all();
+        fail_active(s, st);
         continue;
       }
     }
@@ -248,10 +272,7 @@ void worker_loop(sdg_server* s) {
     s->steps_run += k;
     s->dof_updates += 3.0 * (double)dofs * k;
     if (st != SDG_OK) {
-      s->fatal = st;
-      for (Req* q : s->active) finish(s, q, st);
-      s->active.clear();
-      s->cv_done.notify_all();
+      fail_active(s, st);
       continue;
     }
     std::vector<Req*> still, done;
@@ -284,8 +305,14 @@ void worker_loop(sdg_server* s) {
     if (any_done) {
       s->active.swap(still);
       if (!s->active.empty()) {
+        // the old tables still point at the instances just freed: if they
+        // cannot be rebuilt, no further step may run on them
+        if (s->inject_on_completion) {
+          s->inject_on_completion = false;
+          s->inject_rebuild_failure = true;
+        }
         const int rst = rebuild_tables(s);
-        if (rst != SDG_OK) s->fatal = rst;
+        if (rst != SDG_OK) fail_active(s, rst);
       }
       s->cv_done.notify_all();
     }
@@ -469,6 +496,13 @@ int sdg_server_get_stats(sdg_server* s, sdg_server_stats* out) {
                                    .count()
                              : 0.0;
   out->fatal_status = s->fatal;
+  return SDG_OK;
+}
+
+int sdg_server_inject_rebuild_failure(sdg_server* s) {
+  if (!s) return fail(SDG_ERR_INVALID_ARG, "NULL server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->inject_on_completion = true;
   return SDG_OK;
 }
 

@@ -269,8 +269,7 @@ template <int P>
 int launch_stage_emu_impl(const StageArgs& a, cudaStream_t st) {
   using C = EmuCfg<P>;
   constexpr size_t smem = emu_smem_bytes<P>();
-  SDG_CUDA_TRY(cudaFuncSetAttribute(stage_emu_kernel<P>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SDG_TRY(set_kernel_smem((const void*)stage_emu_kernel<P>, (int)smem, false));
   const long long nblk = (a.elem_count + C::EPB - 1) / C::EPB;
   if (nblk <= 0) return SDG_OK;
   if (nblk > 0x7fffffffLL) return fail(SDG_ERR_INVALID_ARG, "too many elements");

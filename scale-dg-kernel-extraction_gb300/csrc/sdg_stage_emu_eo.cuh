@@ -357,12 +357,7 @@ template <int P>
 int launch_stage_emu_eo_impl(const StageArgs& a, cudaStream_t st) {
   using C = EmuEoCfg<P>;
   constexpr size_t smem = emu_eo_smem_bytes<P>();
-  static bool attr_done = false;
-  if (!attr_done) {
-    SDG_CUDA_TRY(cudaFuncSetAttribute(stage_emu_eo_kernel<P>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_done = true;
-  }
+  SDG_TRY(set_kernel_smem((const void*)stage_emu_eo_kernel<P>, (int)smem, false));
   const long long nblk = (a.elem_count + C::EPB - 1) / C::EPB;
   if (nblk <= 0) return SDG_OK;
   if (nblk > 0x7fffffffLL) return fail(SDG_ERR_INVALID_ARG, "too many elements");

@@ -484,15 +484,7 @@ __global__ void __launch_bounds__(EoCfg<P, CT>::THREADS, eo_min_blocks<P, CT>())
 template <int P, typename CT>
 int launch_stage_eo_impl(const StageArgs& a, cudaStream_t st) {
   constexpr size_t smem = eo_block_smem<P, CT, eo_fly_single<P>()>(EoCfg<P, CT>::EPB);
-  static bool attr_done = false;
-  if (!attr_done) {
-    SDG_CUDA_TRY(cudaFuncSetAttribute(stage_eo_kernel<P, CT>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    SDG_CUDA_TRY(cudaFuncSetAttribute(stage_eo_kernel<P, CT>,
-                                      cudaFuncAttributePreferredSharedMemoryCarveout,
-                                      (int)cudaSharedmemCarveoutMaxShared));
-    attr_done = true;
-  }
+  SDG_TRY(set_kernel_smem((const void*)stage_eo_kernel<P, CT>, (int)smem, true));
   const long long nblk = (a.elem_count + EoCfg<P, CT>::EPB - 1) / EoCfg<P, CT>::EPB;
   if (nblk <= 0) return SDG_OK;
   if (nblk > 0x7fffffffLL) return fail(SDG_ERR_INVALID_ARG, "too many elements");

@@ -165,6 +165,7 @@ def _load() -> C.CDLL:
         "sdg_server_wait": ([_vp, C.c_uint64, _d, C.POINTER(Result)], _i),
         "sdg_server_get_stats": ([_vp, C.POINTER(ServerStats)], _i),
         "sdg_server_reset_stats": ([_vp], _i),
+        "sdg_server_inject_rebuild_failure": ([_vp], _i),
         "sdg_server_destroy": ([_vp], _i),
     }
     for name, (args, res) in sig.items():
@@ -663,6 +664,12 @@ class Server:
 
     def reset_stats(self) -> None:
         _check(lib.sdg_server_reset_stats(self._h), "sdg_server_reset_stats")
+
+    def inject_rebuild_failure(self) -> None:
+        """Host-side fault injection: the next table rebuild after a request
+        completes reports an allocation failure (no device fault)."""
+        _check(lib.sdg_server_inject_rebuild_failure(self._h),
+               "sdg_server_inject_rebuild_failure")
 
     def close(self) -> None:
         if self._h is not None and self._h.value:

@@ -20,12 +20,39 @@ seeded with base seed + instance index.  Arrays are flat, column-major
 from __future__ import annotations
 
 import math
+import os
 
 import numpy as np
 
 BASE_SEED = 20261203
 U0 = (1.0, 0.5, 0.25)
 _M64 = (1 << 64) - 1
+
+# The reference's operator files operator_data/p1..p15.dat, parsed as
+# element_init reads them (mod_mesh.f90:253-263) and stored bit for bit
+# (made by tests/golden/make_operator_data.py).
+OPERATOR_FIXTURE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                "tests", "golden", "operator_data.npz")
+_opcache: dict = {}
+
+
+def reference_operators(p: int):
+    """(x1D, D1D, D1D_tr, Lift_mat) of the reference's operator_data/p{p}.dat,
+    flat column-major float64 arrays, exactly the doubles the reference's
+    list-directed reads produce."""
+    if not 1 <= p <= 15:
+        raise ValueError(f"no operator file for order {p} (the reference ships p1..p15)")
+    if p not in _opcache:
+        with np.load(OPERATOR_FIXTURE) as z:
+            _opcache[p] = tuple(np.ascontiguousarray(z[f"{k}_p{p}"], dtype=np.float64)
+                                for k in ("x1D", "D1D", "D1D_tr", "Lift"))
+    return tuple(a.copy() for a in _opcache[p])
+
+
+def operator_source_digest(p: int) -> str:
+    """sha256 of the operator file the arrays of reference_operators(p) came from."""
+    with np.load(OPERATOR_FIXTURE) as z:
+        return str(z[f"sha256_p{p}"])
 
 
 class SplitMix64:

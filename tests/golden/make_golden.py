@@ -1,9 +1,10 @@
-"""Generates the golden fixtures tests/golden/*.npz with the CPU oracle.
+"""Generates the golden fixtures tests/golden/p*_*.npz with the CPU oracle.
 
-Each fixture is self-contained: it stores the operators, the owned initial
-fields and the oracle's outputs (tendency in OPT1 and GENERAL order, and q
-after nstep SSP-RK3 steps), so that the GPU path and the oracle can be checked
-against it on any machine.  Run from the repository root:
+Each fixture is self-contained: it stores the operators (the reference's own
+operator_data/p{p}.dat, from tests/golden/operator_data.npz), the owned
+initial fields and the oracle's outputs (tendency in OPT1 and GENERAL order,
+and q after nstep SSP-RK3 steps), so that the GPU path and the oracle can be
+checked against it on any machine.  Run from the repository root:
 
     python tests/golden/make_golden.py
 """
@@ -18,20 +19,20 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 sys.path.insert(0, os.path.join(ROOT, "scale-dg-kernel-extraction_gb300"))
 
 import oracle as O  # noqa: E402
-import sdg  # noqa: E402
 import workloads as W  # noqa: E402
 
 CASES = [
     # name, (NeX, NeY, NeZ), p, ic, nstep
     ("p1_sine_4x4x4", (4, 4, 4), 1, "sine", 20),
     ("p3_sine_3x2x4", (3, 2, 4), 3, "sine", 10),
+    ("p7_blob_2x2x2", (2, 2, 2), 7, "blob", 5),
     ("p8_blob_2x1x2", (2, 1, 2), 8, "blob", 4),
 ]
 
 
 def make(name, dims, p, ic, nstep):
     NeX, NeY, NeZ = dims
-    x, D, Dt, L = sdg.operator_generate(p)
+    x, D, Dt, L = W.reference_operators(p)
     m = O.Mesh(NeX, NeY, NeZ, p, x)
     if ic == "sine":
         q, u, v, w = W.sine(NeX, NeY, NeZ, x, (1.0, 0.5, 0.25))

@@ -1,6 +1,7 @@
 """Shared helpers for the tests: building cases and comparing results."""
 from __future__ import annotations
 
+import glob
 import os
 
 import numpy as np
@@ -10,8 +11,9 @@ import workloads as W
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-# The reference's operator files; present only where the reference is mounted.
-REF_OPDATA = "/root/reference/operator_data"
+# the golden cases (inputs and oracle outputs); operator_data.npz holds operators only
+GOLDEN_CASES = sorted(f for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                      if os.path.basename(f) != "operator_data.npz")
 
 # tolerances stated by the parity contract
 TOL_TEND = 1e-12     # relative L2 per tendency (plain FP64 form)
@@ -26,10 +28,19 @@ def rel_l2(x, ref) -> float:
     return float(np.linalg.norm(x - ref) / (den if den > 0 else 1.0))
 
 
-def operators(p: int):
-    """(x1D, D1D, D1D_tr, Lift) from the product's generator."""
-    import sdg
-    return sdg.operator_generate(p)
+def operators(p: int, source: str = "file"):
+    """(x1D, D1D, D1D_tr, Lift) of order p.
+
+    source "file": the reference's own operator_data/p{p}.dat, bit for bit
+    (the committed fixture tests/golden/operator_data.npz); "generated": the
+    product's GLL generator (sdg_operator_generate), which agrees with the
+    files to <= 5e-14."""
+    if source == "file":
+        return W.reference_operators(p)
+    if source == "generated":
+        import sdg
+        return sdg.operator_generate(p)
+    raise ValueError(source)
 
 
 class Case:

@@ -76,3 +76,59 @@ def test_operator_section_counts_each_array_once(monkeypatch):
     assert {c[1][10] for c in lib.calls if c[0] == "sdg_tensorprod_divlike_dirXYZ_dev"} == {1, 2}
     assert names.count("sdg_tensorprod_divlike_dirXYZ_var5_dev") == 3
     assert names.count("sdg_mesh_setup_dev") == 3
+
+
+def test_roofline_counts_algorithmic_bytes_only(monkeypatch):
+    """roofline.frac uses the algorithmic bytes (45.33 B a DOF-update for
+    FP64); the even-odd stage's shared face factors are reported apart."""
+    monkeypatch.setattr(bench, "measured_peaks", lambda: (6000.0, "measured"))
+    p, ne, steps = 7, 32, 10
+    ndof = (p + 1) ** 3 * ne ** 3
+    t = 0.026  # seconds for 10 steps = 30 launches
+    peaks = {"dfma_tflops": 1.25, "ffma_tflops": 75.0}
+    r = bench.roofline("fp64", p, ne, ndof, t, steps, peaks, "evenodd")
+    assert r["algorithmic_bytes_per_dof_update"] == pytest.approx(136 / 3)
+    assert r["implementation_bytes_per_dof_update"] == pytest.approx(12.0)
+    achieved = 136 / 3 * ndof / (t / 30) / 1e9
+    assert r["achieved"] == pytest.approx(achieved)
+    assert r["frac"] == pytest.approx(achieved / 6000.0)
+    assert r["binding_roof"] == "fp64_pipe"
+    assert 0 < r["compute"]["frac"] <= 1.0
+    r32 = bench.roofline("fp32", p, ne, ndof, t, steps, peaks, "evenodd")
+    assert r32["algorithmic_bytes_per_dof_update"] == pytest.approx(100 / 3)
+    assert r32["implementation_bytes_per_dof_update"] == 0
+
+
+def test_headline_line_is_compact(monkeypatch):
+    """The last line the benchmark prints stays under 2 KB with every
+    section present, and carries the contract's keys."""
+    import json
+    monkeypatch.setattr(bench, "measured_peaks", lambda: (6775.3, "measured"))
+    args = types.SimpleNamespace(p=7, ne=32, steps=50, warmup=3, precision="fp64",
+                                 opt="evenodd")
+    ndof = 8 ** 3 * 32 ** 3
+    peaks = {"dfma_tflops": 1.2612345, "ffma_tflops": 75.123456}
+    roof = bench.roofline("fp64", 7, 32, ndof, 0.1303, 50, peaks, "evenodd")
+    cpu = {"value": 0.4234567, "unit": "GDOF-updates/s", "cores": 16, "kind": "port",
+           "sample": "40 SSP-RK3 steps of the same 32^3 p=7 box, OPT1 order (10.1 s; C + "
+                     "OpenMP restatement of the Fortran reference, timing build)"}
+    e2e = {"value": 18.123456, "unit": "GDOF-updates/s", "h2d_bytes_per_step": 536870912,
+           "d2h_bytes_per_step": 134217728, "steps": 50, "path": "x" * 200}
+    clk = {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "samples": 37, "reasons": []}
+    parity = {"tendency_rel_l2_vs_oracle": 1.123456e-14, "tolerance": 1e-12,
+              "state": "initial state, reference operators p7.dat"}
+    srv = {"offered_rate_req_s": 200.0, "solves_per_s": 33.2123, "p50_latency_s": 1.3123,
+           "p99_latency_s": 1.73123, "ratio_vs_plain": 5.2123, "workload": "y" * 300}
+    ens = {"solves_per_s": 443.123, "ratio_vs_plain": 6.7123, "rel_l2_vs_fp64_max": 8.1e-8,
+           "hbm_frac": 0.51234, "autotuned": {"z": "z" * 500}}
+    line = bench.headline_line(args, 1, 19.31234, 0.1303, roof, cpu, e2e, clk, parity,
+                               {"serving_saturated": srv, "ensemble": ens})
+    text = json.dumps(line)
+    assert len(text) <= 2048, len(text)
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "dtype", "config", "roofline", "cpu_baseline", "e2e",
+                "clocks", "parity", "gpu_launches"):
+        assert key in line
+    assert line["gpu_launches"] == 150
+    assert line["config"]["opt"] == "EVENODD"
+    assert bench.config(args, reference=True)["opt"] == "OPT1"

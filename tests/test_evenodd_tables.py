@@ -8,7 +8,7 @@ import pytest
 
 import oracle as O
 import sdg
-from helpers import REF_OPDATA, operators
+from helpers import operators
 
 
 def apply_tables(tab, N, F, gm, gp):
@@ -60,16 +60,17 @@ def check_tables(p, D, L):
 
 @pytest.mark.parametrize("p", range(1, 16))
 def test_tables_reproduce_derivative_and_lift(p):
+    """The reference's operator files have the symmetries to 2.4e-14 (p = 15):
+    the tables build from them and reproduce their D1D and lift columns."""
     x, D, Dt, L = operators(p)
     check_tables(p, D, L)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_OPDATA), reason="reference operator_data not mounted")
 @pytest.mark.parametrize("p", range(1, 16))
-def test_tables_of_the_reference_operator_files(p):
-    """The reference's operator files have the symmetries to 2.4e-14 (p = 15):
-    the tables build from them and reproduce their D1D and lift columns."""
-    x, D, Dt, L = O.read_operator_file(os.path.join(REF_OPDATA, f"p{p}.dat"), p)
+def test_tables_of_the_generated_operators(p):
+    """The generator's operators have the symmetries exactly: the tables build
+    from them and reproduce their D1D and lift columns."""
+    x, D, Dt, L = operators(p, "generated")
     check_tables(p, D, L)
 
 

@@ -11,7 +11,7 @@ import pytest
 import oracle as O
 import sdg
 import workloads as W
-from helpers import GOLDEN, TOL_FP32, TOL_RUN, TOL_TEND, Case, operators, rel_l2
+from helpers import GOLDEN, GOLDEN_CASES, TOL_FP32, TOL_RUN, TOL_TEND, Case, operators, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -39,6 +39,51 @@ def test_fused_stage_tendency_matches_oracle(p, opt):
     dq = s.tendency()
     ref = c.oracle_tend(sdg.OPT_GENERAL if opt == sdg.OPT_GENERAL else sdg.OPT_OPT1)
     assert rel_l2(dq, ref) <= TOL_TEND
+
+
+OP_SOURCES = ["file", "generated"]
+
+
+@pytest.mark.parametrize("p", [1, 3, 7, 8, 15])
+@pytest.mark.parametrize("source", OP_SOURCES)
+@pytest.mark.parametrize("opt,prec", [(sdg.OPT_OPT1, sdg.PREC_FP64),
+                                      (sdg.OPT_GENERAL, sdg.PREC_FP64),
+                                      (sdg.OPT_EVENODD, sdg.PREC_FP64),
+                                      (sdg.OPT_OPT1, sdg.PREC_FP64_EMU),
+                                      (sdg.OPT_EVENODD, sdg.PREC_FP64_EMU)])
+def test_fp64_forms_on_both_operator_sources(p, source, opt, prec):
+    """Every FP64-state form (the fused stage in OPT1, GENERAL and even-odd
+    order, the emulated stage in line and even-odd form) against the oracle,
+    on the reference's own operator_data/p{p}.dat and on the generator's
+    operators: <= 1e-12 per tendency and <= 1e-10 after nstep."""
+    c = Case(*mesh_dims(p), p, ic="blob", ops=operators(p, source))
+    oopt = O.GENERAL if opt == sdg.OPT_GENERAL else O.OPT1
+    s = solver_for(c, opt=opt, prec=prec)
+    assert rel_l2(s.tendency(), c.oracle_tend(oopt)) <= TOL_TEND
+    nstep = 6 if p < 15 else 3
+    s.step(c.dt, nstep)
+    assert rel_l2(s.download(), c.oracle_run(nstep, oopt)) <= TOL_RUN
+
+
+@pytest.mark.parametrize("p", [1, 3, 7, 8, 15])
+@pytest.mark.parametrize("source", OP_SOURCES)
+@pytest.mark.parametrize("opt", ["OPT1", "GENERAL", "EVENODD"])
+def test_dropin_cal_tend_on_both_operator_sources(p, source, opt):
+    """The reference-shaped cal_tend (VMap gathers, the caller's geometry) on
+    the reference's operator files and on the generator's operators."""
+    c = Case(*mesh_dims(p), p, ic="blob", ops=operators(p, source))
+    m = c.mesh
+    sdg.dg_optr_kernel_setup(opt)
+    try:
+        dqdt = np.full(m.Np * m.NeA, 7.0)
+        sdg.advect3d_eq_cal_tend(dqdt, c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, m.VMapM, m.VMapP,
+                                 m.normal_fn, m.Escale, m.Fscale, m.Nq, m.Np, m.NfpTot, m.Ne,
+                                 m.NeA)
+    finally:
+        sdg.dg_optr_kernel_setup("OPT1")
+    ref = c.oracle_tend(O.GENERAL if opt == "GENERAL" else O.OPT1)
+    assert rel_l2(dqdt[: c.nown], ref) <= TOL_TEND
+    assert np.all(dqdt[c.nown:] == 7.0)
 
 
 @pytest.mark.parametrize("p", [1, 4, 7, 12])
@@ -575,7 +620,7 @@ def test_fp32_compute_form_error_and_mass(p, opt):
     assert abs(W.mass(q, c.x1D, c.NeX, c.NeY, c.NeZ) - m0) <= 1e-6 * abs(m0)
 
 
-GOLDEN_FILES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+GOLDEN_FILES = GOLDEN_CASES
 
 
 @pytest.mark.parametrize("path", GOLDEN_FILES, ids=[os.path.basename(p) for p in GOLDEN_FILES])

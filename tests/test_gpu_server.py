@@ -185,3 +185,38 @@ def test_wait_is_bounded(ops):
     assert e.value.status == sdg.ERR_TIMEOUT
     assert srv.wait(t, timeout_s=600)[0]["status"] == 0
     srv.close()
+
+
+def test_failed_rebuild_after_a_completion_fails_the_active_requests(ops):
+    """Host-side fault injection: when the device tables cannot be rebuilt
+    after a request completes, the other active requests (whose old tables
+    point at the freed instance) end with the error, the server records it,
+    and no further step runs for them.  No device fault is involved."""
+    srv = sdg.Server(ops, max_window_steps=4)
+    long_req = req((4, 4, 4), 3, 100000, 71)
+    t_long = srv.submit(**long_req)
+    deadline = time.time() + 60
+    while srv.stats()["active"] < 1:
+        assert time.time() < deadline
+        time.sleep(0.001)
+    srv.inject_rebuild_failure()
+    t_short = srv.submit(**req((2, 2, 2), 3, 3, 72), want_state=True)
+    res, q = srv.wait(t_short, timeout_s=120)
+    assert res["status"] == 0 and q is not None and np.all(np.isfinite(q))
+    with pytest.raises(sdg.SdgError) as e:
+        srv.wait(t_long, timeout_s=120)
+    assert e.value.status == sdg.ERR_OUT_OF_MEMORY
+    st = srv.stats()
+    assert st["fatal_status"] == sdg.ERR_OUT_OF_MEMORY
+    assert st["active"] == 0
+    steps = st["steps_run"]
+    time.sleep(0.2)
+    assert srv.stats()["steps_run"] == steps  # nothing is launched any more
+    # the server still admits and serves new requests afterwards
+    r = req((2, 3, 2), 5, 6, 73)
+    res2, q2 = srv.wait(srv.submit(**r, want_state=True))
+    assert res2["status"] == 0
+    srv.close()
+    alone = sdg.Server(ops)
+    assert np.array_equal(alone.wait(alone.submit(**r, want_state=True))[1], q2)
+    alone.close()

@@ -2,6 +2,8 @@
 against known answers of the mathematics, and against the committed golden
 fixtures.  No GPU is needed."""
 import glob
+import hashlib
+import importlib.util
 import math
 import os
 
@@ -10,9 +12,19 @@ import pytest
 
 import oracle as O
 import workloads as W
-from helpers import GOLDEN, REF_OPDATA, Case, operators, rel_l2
+from helpers import GOLDEN, GOLDEN_CASES, Case, operators, rel_l2
 
-HAVE_REF = os.path.isdir(REF_OPDATA)
+
+def _fixture_script():
+    spec = importlib.util.spec_from_file_location(
+        "make_operator_data", os.path.join(GOLDEN, "make_operator_data.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+MOD = _fixture_script()
+HAVE_REF = os.path.isdir(MOD.REFERENCE_OPERATOR_DIR)
 
 
 def write_opfile(path, x, D, L):
@@ -24,33 +36,46 @@ def write_opfile(path, x, D, L):
 
 # ---- operator data ------------------------------------------------------------
 
-@pytest.mark.skipif(not HAVE_REF, reason="reference operator_data not mounted")
 @pytest.mark.parametrize("p", range(1, 16))
-def test_reference_operator_files_parse(p):
-    x, D, Dt, L = O.read_operator_file(os.path.join(REF_OPDATA, f"p{p}.dat"), p)
+def test_reference_operator_data_properties(p):
+    """The reference's operators (the committed fixture of operator_data/p*.dat):
+    GLL end points, D1D_tr the transpose, D1D annihilates constants."""
+    x, D, Dt, L = operators(p)
     Nq = p + 1
+    assert x.size == Nq and D.size == Nq * Nq and L.size == 6 * Nq ** 3
     assert x[0] == -1.0 and x[-1] == 1.0 and np.all(np.diff(x) > 0)
     assert np.array_equal(Dt.reshape(Nq, Nq), D.reshape(Nq, Nq).T)
-    # D1D annihilates constants (row sums), the property the operators rely on
     assert np.max(np.abs(D.reshape(Nq, Nq, order="F").sum(axis=1))) < 1e-12 * np.abs(D).max()
 
 
-@pytest.mark.skipif(not HAVE_REF, reason="reference operator_data not mounted")
 @pytest.mark.parametrize("p", range(1, 16))
 def test_generated_operators_match_reference_files(p):
     """The product's GLL operator generator reproduces operator_data/p*.dat."""
-    x, D, Dt, L = O.read_operator_file(os.path.join(REF_OPDATA, f"p{p}.dat"), p)
-    gx, gD, gDt, gL = operators(p)
+    x, D, Dt, L = operators(p, "file")
+    gx, gD, gDt, gL = operators(p, "generated")
     assert np.max(np.abs(gx - x)) <= 4e-16
     assert np.max(np.abs(gD - D)) <= 2e-14 * np.abs(D).max()
     assert np.max(np.abs(gL - L)) <= 5e-14 * np.abs(L).max()
 
 
 @pytest.mark.skipif(not HAVE_REF, reason="reference operator_data not mounted")
+@pytest.mark.parametrize("p", range(1, 16))
+def test_operator_fixture_is_the_reference_files(p):
+    """tests/golden/operator_data.npz holds, bit for bit, what the oracle's
+    list-directed reader gives for the reference's files, and records their
+    digests."""
+    path = MOD.source_path(p)
+    with open(path, "rb") as f:
+        assert hashlib.sha256(f.read()).hexdigest() == W.operator_source_digest(p)
+    for a, b in zip(O.read_operator_file(path, p), operators(p, "file")):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.skipif(not HAVE_REF, reason="reference operator_data not mounted")
 @pytest.mark.parametrize("p", [1, 3, 7, 8, 15])
 def test_product_reader_matches_oracle_reader_on_reference_files(p):
     import sdg
-    path = os.path.join(REF_OPDATA, f"p{p}.dat")
+    path = MOD.source_path(p)
     a = O.read_operator_file(path, p)
     b = sdg.operator_read(path, p)
     for u, v in zip(a, b):
@@ -300,7 +325,7 @@ def test_divlike_var5_is_five_opt1_divlikes(p):
 
 # ---- golden fixtures ---------------------------------------------------------------
 
-GOLDEN_FILES = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+GOLDEN_FILES = GOLDEN_CASES
 
 
 def test_golden_fixtures_exist():
