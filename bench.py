@@ -253,10 +253,9 @@ def config(args, reference: bool = False) -> dict:
             "p": args.p, "Ne": [args.ne] * 3, "dof": ndof,
             "opt": "OPT1" if reference else args.opt.upper(),
             "precision": "fp64" if reference else args.precision,
-            "operators": f"operator_data/p{args.p}.dat (the reference's file, bit for bit)",
-            "l2": f"inputs larger than L2 (state+velocity working set {ws_bytes / 1e6:.0f} MB "
-                  "vs 129 MB L2)",
-            "parallelism": "replicas (one independent box per GPU)"}
+            "operators": f"reference operator_data/p{args.p}.dat",
+            "l2": f"inputs > L2 ({ws_bytes / 1e6:.0f} MB working set, 129 MB L2)",
+            "parallelism": "replicas"}
 
 
 OPTS = {"general": 1, "opt1": 2, "evenodd": 3}
@@ -910,9 +909,8 @@ def run_ours(args, ws, rank, local):
             steps, secs = ob.time_steps(args.cpu_seconds, 10 ** 6)
             cpu = {"value": ndof * 3 * steps / secs / 1e9, "unit": "GDOF-updates/s",
                    "cores": ob.threads, "kind": "port",
-                   "sample": f"{steps} SSP-RK3 steps of the same {ne}^3 p={p} box, OPT1 "
-                             f"order ({secs:.1f} s; C + OpenMP restatement of the Fortran "
-                             "reference, timing build)"}
+                   "sample": f"{steps} SSP-RK3 steps of the same box, OPT1 order, "
+                             f"{secs:.1f} s (C+OpenMP restatement of the reference)"}
     if other is not None:
         emit_section("fp64_emulated", other, sections)
     if ws == 1 and not args.no_dropin:

@@ -61,6 +61,16 @@ class Case:
             m.update_halo(f)
         self.dt = W.cfl_dt(NeX, NeY, NeZ, p, u, v, w)
 
+    def term_scale(self) -> float:
+        """Size of the terms the tendency sums (Escale |D| |q| |u| over the
+        owned nodes): the floor of a relative error whose exact result
+        vanishes, as at p = 1 on a one-element periodic box, where all eight
+        nodes are the same point and the tendency is rounding noise."""
+        n = self.nown
+        vmax = max(np.abs(a[:n]).max() for a in (self.u, self.v, self.w))
+        es = max(self.NeX, self.NeY, self.NeZ) * 2.0
+        return float(es * np.abs(self.D).max() * vmax * np.linalg.norm(self.q[:n]))
+
     @property
     def nown(self) -> int:
         return self.mesh.Np * self.mesh.Ne

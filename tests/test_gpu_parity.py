@@ -100,7 +100,13 @@ def test_single_element_box_is_its_own_neighbour(p, opt, prec, tol):
     c = Case(1, 1, 1, p, ic="blob")
     s = solver_for(c, opt=opt, prec=prec)
     ref = c.oracle_tend(sdg.OPT_GENERAL if opt == sdg.OPT_GENERAL else sdg.OPT_OPT1)
-    assert rel_l2(s.tendency(), ref) <= tol
+    # at p = 1 the exact tendency of this box is zero (all nodes coincide) and
+    # the oracle's is rounding noise: measure the error against the size of
+    # the terms then, against the tendency otherwise
+    den = np.linalg.norm(ref)
+    if den < 1e-6 * c.term_scale():
+        den = c.term_scale()
+    assert np.linalg.norm(s.tendency() - ref) / den <= tol
     s.step(c.dt, 3)
     assert rel_l2(s.download(), c.oracle_run(3)) <= (TOL_RUN if tol == TOL_TEND else tol)
 
