@@ -641,6 +641,66 @@ def bench_dropin(sdg, args, wl, fused_rate, opt=None):
             "achieved_gbs_with_geometry": bpd * rate}
 
 
+def bench_dropin_step(sdg, args, wl, fused_rate, opt=None):
+    """The time loop on the reference's arrays in one call
+    (sdg_advect3d_eq_step_dev): mesh arrays built on the device, then K
+    SSP-RK3 steps; EVENODD runs one fused launch a stage (face flux from
+    VMapM/VMapP, normal_fn and Fscale, per-node Escale, lift, RK update),
+    OPT1 the reference's per-stage sequence.  Timed on the host around the
+    call with a synchronize on both sides."""
+    opt = sdg.OPT_EVENODD if opt is None else opt
+    p, ne = args.p, args.ne
+    nq, np_ = p + 1, (p + 1) ** 3
+    ntf = 6 * nq * nq
+    ne3 = ne ** 3
+    nhalo = 6 * ne * ne
+    nea = ne3 + nhalo
+    nhn = nq * nq * nhalo
+    lib = sdg.lib
+    A = sdg.DeviceArray
+    vm, vp = A(n=ntf * ne3, dtype=np.int32), A(n=ntf * ne3, dtype=np.int32)
+    nf, fs = A(n=3 * ntf * ne3), A(n=ntf * ne3)
+    es, hm = A(n=3 * np_ * ne3), A(n=nhn, dtype=np.int32)
+    sdg._check(lib.sdg_mesh_setup_dev(ne, ne, ne, p, 1.0, 1.0, 1.0, None, vm.ptr, vp.ptr, nf.ptr,
+                                      es.ptr, fs.ptr, None, hm.ptr, None), "sdg_mesh_setup_dev")
+    fields = []
+    for key in ("q", "u", "v", "w"):
+        h = np.zeros(np_ * nea)
+        h[: np_ * ne3] = wl[key]
+        d = A(h)
+        sdg._check(lib.sdg_update_halo_dev(d.ptr, hm.ptr, np_, ne3, nhn, None), "update_halo")
+        fields.append(d)
+    q, u, v, w = fields
+    D, Dt, L = A(wl["D"]), A(wl["Dt"]), A(wl["L"])
+    nbytes = int(lib.sdg_advect3d_eq_step_scratch_bytes(nq, ne3))
+    scratch = A(n=nbytes, dtype=np.uint8)
+    err = A(np.zeros(1, dtype=np.int32))
+
+    def run(k):
+        sdg._check(lib.sdg_advect3d_eq_step_dev(
+            q.ptr, u.ptr, v.ptr, w.ptr, D.ptr, Dt.ptr, L.ptr, vm.ptr, vp.ptr, nf.ptr, es.ptr,
+            fs.ptr, hm.ptr, nq, np_, ntf, ne3, nea, nhn, wl["dt"], k, opt, scratch.ptr, nbytes,
+            err.ptr, None), "sdg_advect3d_eq_step_dev")
+
+    run(args.warmup)
+    sdg.synchronize()
+    k = max(2, min(args.steps, 20))
+    t0 = time.perf_counter()
+    run(k)
+    sdg.synchronize()
+    t = time.perf_counter() - t0
+    assert err.numpy()[0] == 0
+    rate = np_ * ne3 * 3 * k / t / 1e9
+    oname = {sdg.OPT_OPT1: "OPT1 order, the reference's per-stage sequence",
+             sdg.OPT_EVENODD: "one fused even-odd launch a stage"}[opt]
+    return {"workload": f"same {ne}^3 p={p} box, sdg_advect3d_eq_step_dev on the reference's "
+                        f"arrays (VMapM/VMapP, halo_src_map, normal_fn, Escale, Fscale), {oname}",
+            "gdof_updates_per_s": rate, "ms_per_step": 1e3 * t / k, "steps": k,
+            "launches_per_step": 3 if opt == sdg.OPT_EVENODD else 13,
+            "ratio_to_fused_structured_stage": rate / fused_rate,
+            "scratch_bytes": nbytes}
+
+
 def bench_serving(sdg, args, rate=None, plain_cache=None):
     """Poisson arrivals of solves (Ne per axis U{4..32}, p U{2..11}, nstep
     U{10..500}, Gaussian tracer in a constant velocity, FP32 compute / FP64
@@ -916,6 +976,9 @@ def run_ours(args, ws, rank, local):
     if ws == 1 and not args.no_dropin:
         emit_section("dropin", bench_dropin(sdg, args, wl, value), sections)
         emit_section("dropin_evenodd", bench_dropin(sdg, args, wl, value, sdg.OPT_EVENODD),
+                     sections)
+        emit_section("dropin_step", bench_dropin_step(sdg, args, wl, value), sections)
+        emit_section("dropin_step_opt1", bench_dropin_step(sdg, args, wl, value, sdg.OPT_OPT1),
                      sections)
     if ws == 1 and not args.no_operators:
         emit_section("operators", bench_operators(sdg, args, peaks), sections)

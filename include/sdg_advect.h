@@ -283,6 +283,40 @@ int sdg_update_halo_dev(double* f, const int* halo_src_map, int Np, int Ne,
 int sdg_rk_stage_dev(double* q, const double* q0, const double* dqdt, int Np,
                      int Ne, int stage, double dt, void* stream);
 
+/* The time loop of main.f90:51-80 on the reference's own device arrays:
+ * nstep SSP-RK3 steps of q (Np*NeA; the owned part is advanced), each step
+ * q0 = q and per stage update_halo(q) (mod_mesh.f90:209-221),
+ * advect3d_eq_cal_tend (mod_advect3d_eq.f90:41-85) and the RK update
+ * (main.f90:68-73).  Every array has its reference meaning and layout, as in
+ * sdg_advect3d_eq_cal_tend_dev, plus halo_src_map (NhaloNode, 1-based) for
+ * the halo slots that VMapP points into.
+ *   opt SDG_OPT_EVENODD: one fused launch per stage on two scratch state
+ *     buffers -- face flux from VMapM / VMapP, normal_fn and Fscale, the
+ *     even-odd line sums with the caller's per-node Escale, the lift and the
+ *     RK update.  Halo slots are resolved through halo_src_map once per call
+ *     instead of being copied every stage; the velocity factors of the face
+ *     flux are formed in a step's first stage and reused in its other two.
+ *   opt SDG_OPT_OPT1 / SDG_OPT_GENERAL: the reference's sequence and
+ *     summation order (q0 copy, halo update, flux, cal_dqdt, RK: 13 launches
+ *     a step).
+ * scratch: device memory of at least sdg_advect3d_eq_step_scratch_bytes(Nq,
+ * Ne) bytes, 256-byte aligned.  Errors found on the device set *err_flag
+ * (not cleared here): 1 for a VMapM / VMapP / halo_src_map entry outside the
+ * DOFs it may name, 2 for operators without the even-odd symmetries.  On
+ * return the halo slots of q hold the final state's halo values.  Runs
+ * asynchronously on `stream`. */
+size_t sdg_advect3d_eq_step_scratch_bytes(int Nq, int Ne);
+int sdg_advect3d_eq_step_dev(double* q, const double* u, const double* v,
+                             const double* w, const double* D1D,
+                             const double* D1D_tr, const double* Lift_mat,
+                             const int* VMapM, const int* VMapP,
+                             const double* normal_fn, const double* Escale,
+                             const double* Fscale, const int* halo_src_map,
+                             int Nq, int Np, int NfpTot, int Ne, int NeA,
+                             int NhaloNode, double dt, int nstep, int opt,
+                             void* scratch, size_t scratch_bytes,
+                             int* err_flag, void* stream);
+
 /* ---- device-resident solver (replaces the time loop of main.f90:51-80) -- */
 
 /* A periodic structured box of NeX x NeY x NeZ hexahedra of order p on

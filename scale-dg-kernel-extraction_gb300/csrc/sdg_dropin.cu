@@ -2,6 +2,7 @@
 // update_halo and the RK combine, on host or device pointers.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <cstring>
 #include <vector>
 
@@ -150,6 +151,45 @@ __global__ void rk_kernel(double* q, const double* q0, const double* dqdt,
     // main.f90:70-71: rk_a*q0 + rk_b*(q + dt*dqdt)
     const double r = b * (q[i] + dt * dqdt[i]);
     q[i] = (a != 0.0) ? a * q0[i] + r : r;
+  }
+}
+
+// Once per call, one thread per face node m: the owned nodes its qM and qP
+// come from (VMapM(m), VMapP(m), a halo slot b followed through
+// halo_src_map(b)) and the velocity factors (tP, tM) of its flux from the
+// caller's velocity at VMapM / VMapP, normal_fn and Fscale.  An entry out of
+// range sets *err = 1 and gives the face node a zero flux.
+__global__ void step_face_kernel(const int* __restrict__ VMapM, const int* __restrict__ VMapP,
+                                 const int* __restrict__ halo_src_map,
+                                 const double* __restrict__ u, const double* __restrict__ v,
+                                 const double* __restrict__ w,
+                                 const double* __restrict__ normal_fn,
+                                 const double* __restrict__ Fscale, int2* res, double2* fc,
+                                 long long NT, long long NpNe, long long NpNeA,
+                                 long long NhaloNode, int* err) {
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < NT;
+       m += (long long)gridDim.x * blockDim.x) {
+    const long long vM = (long long)VMapM[m] - 1, vP = (long long)VMapP[m] - 1;
+    long long r[2] = {vM, vP};
+#pragma unroll
+    for (int side = 0; side < 2; side++)
+      if (r[side] >= NpNe && r[side] < NpNeA && r[side] - NpNe < NhaloNode)
+        r[side] = (long long)halo_src_map[r[side] - NpNe] - 1;
+    const bool ok = vM >= 0 && vM < NpNeA && vP >= 0 && vP < NpNeA && r[0] >= 0 &&
+                    r[0] < NpNe && r[1] >= 0 && r[1] < NpNe;
+    if (!ok) {
+      atomicExch(err, 1);
+      res[m] = make_int2(-1, -1);
+      fc[m] = make_double2(0.0, 0.0);
+      continue;
+    }
+    res[m] = make_int2((int)r[0], (int)r[1]);
+    const double n1 = normal_fn[m], n2 = normal_fn[m + NT], n3 = normal_fn[m + 2 * NT];
+    const double velM = u[vM] * n1 + v[vM] * n2 + w[vM] * n3;
+    const double velP = u[vP] * n1 + v[vP] * n2 + w[vP] * n3;
+    const double alpha = 0.5 * fabs(velP + velM);
+    const double hf = 0.5 * Fscale[m];
+    fc[m] = make_double2(hf * (velP - alpha), hf * (velM - alpha));
   }
 }
 
@@ -465,6 +505,139 @@ int sdg_rk_stage_dev(double* q, const double* q0, const double* dqdt, int Np,
   rk_kernel<<<grid_for(n), 256, 0, as_stream(stream)>>>(q, q0, dqdt, n, rk_a[stage - 1],
                                                        rk_b[stage - 1], dt);
   SDG_CUDA_TRY(cudaGetLastError());
+  return SDG_OK;
+}
+
+// ---- the time loop on the reference's arrays ---------------------------------
+
+// Scratch of sdg_advect3d_eq_step_dev, 256-byte aligned pieces: two stage
+// states (Np*Ne), the face factors (tP, tM) per face node, the resolved
+// gather indices (M, P) per face node, and the even-odd tables.
+static size_t step_layout(int Nq, long long Ne, size_t off[5]) {
+  const long long np = (long long)Nq * Nq * Nq, nft = 6LL * Nq * Nq * Ne;
+  const int N = Nq, H = N / 2, HR = (N + 1) / 2;
+  const long long te = (long long)H * H + (long long)HR * H + (N & 1) * H + HR + H;
+  const size_t sizes[5] = {(size_t)(8 * np * Ne), (size_t)(8 * np * Ne), (size_t)(16 * nft),
+                           (size_t)(8 * nft), (size_t)(8 * 3 * te)};
+  size_t total = 0;
+  for (int k = 0; k < 5; k++) {
+    off[k] = total;
+    total += (sizes[k] + 255) & ~size_t(255);
+  }
+  return total;
+}
+
+size_t sdg_advect3d_eq_step_scratch_bytes(int Nq, int Ne) {
+  if (Nq - 1 < 1 || Nq - 1 > kMaxOrder || Ne < 0) return 0;
+  size_t off[5];
+  return step_layout(Nq, Ne, off);
+}
+
+int sdg_advect3d_eq_step_dev(double* q, const double* u, const double* v, const double* w,
+                             const double* D1D, const double* D1D_tr, const double* Lift_mat,
+                             const int* VMapM, const int* VMapP, const double* normal_fn,
+                             const double* Escale, const double* Fscale,
+                             const int* halo_src_map, int Nq, int Np, int NfpTot, int Ne,
+                             int NeA, int NhaloNode, double dt, int nstep, int opt,
+                             void* scratch, size_t scratch_bytes, int* err_flag,
+                             void* stream) {
+  // RK3 SSP coefficients, mod_common.f90:28-30
+  static const double rk_a[3] = {0.0, 0.75, 1.0 / 3.0};
+  static const double rk_b[3] = {1.0, 0.25, 2.0 / 3.0};
+  SDG_TRY(check_opt(opt));
+  SDG_TRY(check_tend_shape(Nq, Np, NfpTot, Ne, NeA));
+  if (nstep < 0 || NhaloNode < 0)
+    return fail(SDG_ERR_INVALID_ARG, "nstep %d / NhaloNode %d negative", nstep, NhaloNode);
+  if ((long long)Np * NeA > 0x7fffffffLL)
+    return fail(SDG_ERR_INVALID_ARG, "Np*NeA beyond the 32-bit DOF ids of VMapM/VMapP");
+  if (Ne == 0 || nstep == 0) return SDG_OK;
+  size_t off[5];
+  const size_t need = step_layout(Nq, Ne, off);
+  if (!scratch || scratch_bytes < need)
+    return fail(SDG_ERR_INVALID_ARG, "scratch of %zu bytes, %zu needed "
+                "(sdg_advect3d_eq_step_scratch_bytes)", scratch_bytes, need);
+  if (!q || !u || !v || !w || !D1D || !D1D_tr || !Lift_mat || !VMapM || !VMapP ||
+      !normal_fn || !Escale || !Fscale || !err_flag || (NhaloNode > 0 && !halo_src_map))
+    return fail(SDG_ERR_INVALID_ARG, "NULL device pointer");
+  if ((reinterpret_cast<uintptr_t>(scratch) & 255) != 0)
+    return fail(SDG_ERR_INVALID_ARG, "scratch must be 256-byte aligned");
+  cudaStream_t st = as_stream(stream);
+  char* base = static_cast<char*>(scratch);
+  double* qB = reinterpret_cast<double*>(base + off[0]);
+  double* qC = reinterpret_cast<double*>(base + off[1]);
+  const long long np = Np, nft = (long long)NfpTot * Ne, npne = np * Ne;
+  const int p = Nq - 1;
+
+  if (opt != SDG_OPT_EVENODD) {
+    // the reference's own sequence and summation order: q0 = q, then per
+    // stage update_halo(q), cal_tend into dqdt, the RK update (main.f90:51-80)
+    double* flux = reinterpret_cast<double*>(base + off[2]);
+    TendArgs ta{qC, q, u, v, w, D1D, D1D_tr, Lift_mat, VMapM, VMapP, normal_fn,
+                Escale, Fscale, flux, err_flag, Ne, np * NeA};
+    for (int s = 0; s < nstep; s++) {
+      SDG_CUDA_TRY(cudaMemcpyAsync(qB, q, 8 * npne, cudaMemcpyDeviceToDevice, st));
+      for (int stage = 0; stage < 3; stage++) {
+        if (NhaloNode > 0) {
+          update_halo_kernel<<<grid_for(NhaloNode), 256, 0, st>>>(q, halo_src_map, npne,
+                                                                 NhaloNode, npne, err_flag);
+          SDG_CUDA_TRY(cudaGetLastError());
+        }
+        SDG_TRY(tend_dev(ta, p, NfpTot, opt, st));
+        rk_kernel<<<grid_for(npne), 256, 0, st>>>(q, qB, qC, npne, rk_a[stage], rk_b[stage],
+                                                   dt);
+        SDG_CUDA_TRY(cudaGetLastError());
+      }
+    }
+    // leave the halo slots of q consistent with the final state
+    if (NhaloNode > 0) {
+      update_halo_kernel<<<grid_for(NhaloNode), 256, 0, st>>>(q, halo_src_map, npne, NhaloNode,
+                                                             npne, err_flag);
+      SDG_CUDA_TRY(cudaGetLastError());
+    }
+    return SDG_OK;
+  }
+
+  // even-odd: the per-call face data, then one fused launch per stage on
+  // ping-pong buffers
+  double2* fc = reinterpret_cast<double2*>(base + off[2]);
+  int2* res = reinterpret_cast<int2*>(base + off[3]);
+  double* tab = reinterpret_cast<double*>(base + off[4]);
+  StepTablesArgs tb{D1D, D1D_tr, Lift_mat, tab, err_flag};
+  SDG_TRY(dropin(p, 5, opt, &tb, st));
+  step_face_kernel<<<grid_for(nft), 256, 0, st>>>(VMapM, VMapP, halo_src_map, u, v, w,
+                                                  normal_fn, Fscale, res, fc, nft, npne,
+                                                  np * NeA, NhaloNode, err_flag);
+  SDG_CUDA_TRY(cudaGetLastError());
+  StepRefArgs a{};
+  a.u = u;
+  a.v = v;
+  a.w = w;
+  a.tab = tab;
+  a.res = res;
+  a.fc = fc;
+  a.Escale = Escale;
+  a.Ne = Ne;
+  for (int s = 0; s < nstep; s++) {
+    // stage 1: q -> B; 2: B, q0 = q -> C; 3: C, q0 = q -> q
+    const double* ins[3] = {q, qB, qC};
+    double* outs[3] = {qB, qC, q};
+    for (int stage = 0; stage < 3; stage++) {
+      a.q_in = ins[stage];
+      a.q0 = q;
+      a.q_out = outs[stage];
+      a.a = rk_a[stage];
+      a.b = rk_b[stage];
+      a.c = -rk_b[stage] * dt;
+      a.rk = stage == 0 ? kRkFirst : kRkGeneral;
+      SDG_TRY(dropin(p, 4, opt, &a, st));
+    }
+  }
+  // leave the halo slots of q consistent with the final state
+  if (NhaloNode > 0) {
+    update_halo_kernel<<<grid_for(NhaloNode), 256, 0, st>>>(q, halo_src_map, npne, NhaloNode,
+                                                           npne, err_flag);
+    SDG_CUDA_TRY(cudaGetLastError());
+  }
   return SDG_OK;
 }
 

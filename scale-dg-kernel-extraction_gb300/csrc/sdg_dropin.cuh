@@ -475,7 +475,24 @@ int launch_lift_impl(double* out, const double* Lift, const double* in, int nele
   return SDG_OK;
 }
 
-// Per-order entry used by the dispatch in sdg_dropin.cu.
+}  // namespace sdg
+
+#include "sdg_dropin_step.cuh"
+
+namespace sdg {
+
+// Tables of the fused reference-array stage (one block, symmetry checks).
+struct StepTablesArgs {
+  const double* D;
+  const double* Dt;
+  const double* Lift;
+  double* tab;
+  int* err;
+};
+
+// Per-order entry used by the dispatch in sdg_dropin.cu.  what: 0 cal_dqdt,
+// 1 divlike, 2 lift, 3 gradlike, 4 one fused reference-array stage, 5 the
+// tables of that stage.
 template <int P>
 int dropin_order(int what, int opt, const void* args, cudaStream_t st) {
   constexpr bool kCanSplit = (P > 7);
@@ -493,6 +510,14 @@ int dropin_order(int what, int opt, const void* args, cudaStream_t st) {
     }
     case 3:
       return launch_gradlike_impl<P>(*static_cast<const DivArgs*>(args), st);
+    case 4:
+      return launch_step_ref_impl<P>(*static_cast<const StepRefArgs*>(args), st);
+    case 5: {
+      const StepTablesArgs& a = *static_cast<const StepTablesArgs*>(args);
+      step_tables_kernel<P><<<1, 256, 0, st>>>(a.D, a.Dt, a.Lift, a.tab, a.err);
+      SDG_CUDA_TRY(cudaGetLastError());
+      return SDG_OK;
+    }
     default: {
       const DivArgs& a = *static_cast<const DivArgs*>(args);
       // lift: ox = out, D = Lift, ix = in

@@ -115,6 +115,9 @@ def _load() -> C.CDLL:
         "sdg_solver_run": ([_vp, _d, _i, _i, _vp], _i),
         "sdg_mesh_setup_dev": ([_i, _i, _i, _i, _d, _d, _d, _vp] + [_vp] * 7 + [_vp], _i),
         "sdg_rk_stage_dev": ([_vp, _vp, _vp, _i, _i, _i, _d, _vp], _i),
+        "sdg_advect3d_eq_step_scratch_bytes": ([_i, _i], C.c_size_t),
+        "sdg_advect3d_eq_step_dev": ([_vp] * 13 + [_i] * 6 + [_d, _i, _i, _vp, C.c_size_t,
+                                                          _vp, _vp], _i),
         "sdg_solver_create": ([C.POINTER(_vp), _i, _i, _i, _i, _d, _d, _d, _dp, _dp, _i, _i,
                                _vp], _i),
         "sdg_solver_check_mesh": ([_vp, _ip, _ip, _dp, _dp, _dp], _i),
@@ -307,6 +310,36 @@ def tensorprod_Lift_hexahedral(Lift, vec_in, Nq):
     _check(lib.sdg_tensorprod_Lift_hexahedral(out, _f64(Lift), vi, Nq, nelem),
            "tensorprod_Lift_hexahedral")
     return out
+
+
+def advect3d_eq_step(q, u, v, w, D1D, D1D_tr, Lift_mat, VMapM, VMapP, normal_fn, Escale,
+                     Fscale, halo_src_map, Nq, Np, NfpTot, Ne, NeA, NhaloNode, dt, nstep,
+                     opt=OPT_EVENODD):
+    """nstep SSP-RK3 steps of the time loop of main.f90:51-80 on the
+    reference's arrays through sdg_advect3d_eq_step_dev: uploads every array,
+    runs, and returns q (Np*NeA, halo slots refreshed).  Raises SdgError with
+    status ERR_MESH / ERR_INVALID_ARG when the device reports a bad map entry
+    or operators without the even-odd symmetries."""
+    arrs = [DeviceArray(_f64(a)) for a in (q, u, v, w, D1D, D1D_tr, Lift_mat)]
+    maps = [DeviceArray(np.ascontiguousarray(a, dtype=np.int32)) for a in (VMapM, VMapP)]
+    geo = [DeviceArray(_f64(a)) for a in (normal_fn, Escale, Fscale)]
+    hm = DeviceArray(np.ascontiguousarray(halo_src_map, dtype=np.int32)) if NhaloNode > 0 \
+        else None
+    nbytes = int(lib.sdg_advect3d_eq_step_scratch_bytes(Nq, Ne))
+    scratch = DeviceArray(n=max(nbytes, 1), dtype=np.uint8)
+    err = DeviceArray(np.zeros(1, dtype=np.int32))
+    _check(lib.sdg_advect3d_eq_step_dev(
+        arrs[0].ptr, arrs[1].ptr, arrs[2].ptr, arrs[3].ptr, arrs[4].ptr, arrs[5].ptr, arrs[6].ptr,
+        maps[0].ptr, maps[1].ptr, geo[0].ptr, geo[1].ptr, geo[2].ptr,
+        hm.ptr if hm is not None else None, Nq, Np, NfpTot, Ne, NeA, NhaloNode, float(dt),
+        int(nstep), int(opt), scratch.ptr, nbytes, err.ptr, None), "sdg_advect3d_eq_step_dev")
+    flag = int(err.numpy()[0])
+    if flag == 2:
+        raise SdgError(ERR_INVALID_ARG, "advect3d_eq_step",
+                       "operators lack the even-odd symmetries")
+    if flag:
+        raise SdgError(ERR_MESH, "advect3d_eq_step", "a map entry is out of range")
+    return arrs[0].numpy()
 
 
 # ---- device memory for the *_dev entry points ------------------------------

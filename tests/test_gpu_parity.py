@@ -697,3 +697,100 @@ def test_full_size_mass_conservation_and_shift_invariance(full_case, prec, opt):
     s2.upload(shift(f["q"]), shift(f["u"]), shift(f["v"]), shift(f["w"]))
     s2.step(f["dt"], 5)
     assert np.array_equal(s2.download(), shift(q))
+
+
+# ---- the time loop on the reference's arrays (sdg_advect3d_eq_step_dev) --------
+
+def _step_args(c, m=None):
+    m = m or c.mesh
+    return (m.VMapM, m.VMapP, m.normal_fn, m.Escale, m.Fscale, m.halo_src_map, m.Nq, m.Np,
+            m.NfpTot, m.Ne, m.NeA, m.NhaloNode)
+
+
+@pytest.mark.parametrize("p", [1, 3, 7, 8, 15])
+@pytest.mark.parametrize("opt", [sdg.OPT_OPT1, sdg.OPT_GENERAL, sdg.OPT_EVENODD])
+def test_reference_array_step_matches_oracle(p, opt):
+    """nstep steps of main.f90's loop through the reference's own arrays
+    (VMapM/VMapP into halo slots, normal_fn, per-node Escale, Fscale,
+    halo_src_map): the fused even-odd stage and the reference-order sequence
+    against the oracle's loop, <= 1e-10 after nstep; the halo slots of the
+    result hold the final state."""
+    c = Case(*mesh_dims(p), p, ic="blob")
+    nstep = 5 if p < 15 else 2
+    q = sdg.advect3d_eq_step(c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, *_step_args(c), c.dt,
+                             nstep, opt)
+    ref = c.oracle_run(nstep, O.GENERAL if opt == sdg.OPT_GENERAL else O.OPT1)
+    assert rel_l2(q[: c.nown], ref) <= TOL_RUN
+    m = c.mesh
+    assert np.array_equal(q[c.nown: c.nown + m.NhaloNode], q[m.halo_src_map - 1])
+
+
+@pytest.mark.parametrize("opt", [sdg.OPT_OPT1, sdg.OPT_EVENODD])
+def test_reference_array_step_honours_normals_and_escale(opt):
+    """Oblique normals, per-node Escale and per-face-node Fscale that differ
+    from the structured box's: the fused stage uses the caller's arrays."""
+    import copy
+    c = Case(3, 2, 2, 4, ic="blob")
+    m = copy.copy(c.mesh)
+    rng = np.random.default_rng(123)
+    nt = m.NfpTot * m.Ne
+    nf = c.mesh.normal_fn.copy().reshape(3, nt)
+    pick = rng.random(nt) < 0.5
+    nf[:, pick] += 0.2 * rng.standard_normal((3, int(pick.sum())))
+    m.normal_fn = nf.reshape(-1)
+    m.Escale = c.mesh.Escale * (1.0 + 0.2 * rng.random(c.mesh.Escale.size))
+    m.Fscale = c.mesh.Fscale * (1.0 + 0.2 * rng.random(c.mesh.Fscale.size))
+    nstep = 4
+    q = sdg.advect3d_eq_step(c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, *_step_args(c, m), c.dt,
+                             nstep, opt)
+    qq = c.q.copy()
+    O.run(m, qq, c.u, c.v, c.w, c.D, c.Dt, c.Lift, c.dt, nstep, O.OPT1)
+    assert rel_l2(q[: c.nown], qq[: c.nown]) <= TOL_RUN
+
+
+def test_reference_array_step_equals_per_stage_calls():
+    """The fused even-odd step equals the per-stage device calls of the
+    reference's loop (halo, even-odd cal_tend, RK) to rounding."""
+    c = Case(4, 3, 2, 5, ic="blob")
+    a = sdg.advect3d_eq_step(c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, *_step_args(c), c.dt, 3,
+                             sdg.OPT_EVENODD)
+    b = sdg.advect3d_eq_step(c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, *_step_args(c), c.dt, 3,
+                             sdg.OPT_OPT1)
+    assert rel_l2(a, b) <= TOL_RUN
+
+
+def test_reference_array_step_reports_bad_maps_and_scratch():
+    c = Case(2, 2, 2, 3, ic="blob")
+    m = c.mesh
+    bad = m.VMapP.copy()
+    bad[3] = m.Np * m.NeA + 5
+    import copy
+    mb = copy.copy(m)
+    mb.VMapP = bad
+    for opt in (sdg.OPT_EVENODD, sdg.OPT_OPT1):
+        with pytest.raises(sdg.SdgError) as e:
+            sdg.advect3d_eq_step(c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, *_step_args(c, mb), c.dt,
+                                 1, opt)
+        assert e.value.status == sdg.ERR_MESH
+    badmap = m.halo_src_map.copy()
+    badmap[0] = 0
+    mh = copy.copy(m)
+    mh.halo_src_map = badmap
+    with pytest.raises(sdg.SdgError) as e:
+        sdg.advect3d_eq_step(c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, *_step_args(c, mh), c.dt, 1,
+                             sdg.OPT_EVENODD)
+    assert e.value.status == sdg.ERR_MESH
+    badD = c.D.copy()
+    badD[2] *= 1.0 + 1e-9
+    with pytest.raises(sdg.SdgError) as e:
+        sdg.advect3d_eq_step(c.q, c.u, c.v, c.w, badD, badD.reshape(m.Nq, m.Nq).T.reshape(-1),
+                             c.Lift, *_step_args(c), c.dt, 1, sdg.OPT_EVENODD)
+    assert e.value.status == sdg.ERR_INVALID_ARG
+    # a scratch buffer below the stated size is refused before any launch
+    need = sdg.lib.sdg_advect3d_eq_step_scratch_bytes(m.Nq, m.Ne)
+    small = sdg.DeviceArray(n=need // 2, dtype=np.uint8)
+    qd = sdg.DeviceArray(c.q)
+    st = sdg.lib.sdg_advect3d_eq_step_dev(qd.ptr, *[qd.ptr] * 12, m.Nq, m.Np, m.NfpTot, m.Ne,
+                                          m.NeA, m.NhaloNode, c.dt, 1, sdg.OPT_EVENODD,
+                                          small.ptr, need // 2, qd.ptr, None)
+    assert st == sdg.ERR_INVALID_ARG
