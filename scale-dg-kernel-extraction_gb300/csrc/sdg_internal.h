@@ -83,9 +83,9 @@ struct StageArgs {
   // even-odd FP64 stage: the velocity factors of the face flux, (tP, tM) per
   // face node of each element (2*Nfp*6 doubles an element).  A stage with
   // fc_out forms them from u, v, w and stores them; a stage with fc_in reads
-  // them instead (same bits), so the three stages of one RK step, which share
-  // the velocity (main.f90:58-67 passes the same u, v, w to the three
-  // advect3d_eq_cal_tend calls), form them once.  Both null: formed inline.
+  // them instead (same bits), so the stages of one solver call, which share
+  // the velocity (main.f90:58-67 passes the same u, v, w to every
+  // advect3d_eq_cal_tend call), form them once.  Both null: formed inline.
   double* fc_out;
   const double* fc_in;
 };

@@ -85,8 +85,9 @@ void release(sdg_solver* s) {
 }
 
 // fc: 0 = the stage forms the face-flux velocity factors inline, 1 = it also
-// stores them in s->fc, 2 = it reads them from s->fc (a stage of the same
-// step, same velocity, stored them); 1 and 2 apply only when s->fc exists.
+// stores them in s->fc, 2 = it reads them from s->fc (an earlier stage of
+// the same call, same velocity, stored them); 1 and 2 apply only when s->fc
+// exists.
 int one_stage_on(sdg_solver* s, int stage, double dt, const double* qin, const double* q0,
                  double* qout, const void* u, const void* v, const void* w, cudaStream_t st,
                  bool tend_only, int fc = 0);
@@ -417,7 +418,10 @@ int sdg_solver_step(sdg_solver* s, double dt, int nstep) {
   if (nstep < 0) return fail(SDG_ERR_INVALID_ARG, "nstep < 0");
   for (int it = 0; it < nstep; it++) {
     const int s0 = s->cur, s1 = (s->cur + 1) % 3, s2 = (s->cur + 2) % 3;
-    SDG_TRY(one_stage(s, 0, dt, s->q[s0], nullptr, s->q[s1], false, 1));
+    // the velocity cannot change within one call: the first stage of the
+    // call forms the face-flux velocity factors and every later stage of the
+    // call reads them (a velocity uploaded between calls is formed afresh)
+    SDG_TRY(one_stage(s, 0, dt, s->q[s0], nullptr, s->q[s1], false, it == 0 ? 1 : 2));
     SDG_TRY(one_stage(s, 1, dt, s->q[s1], s->q[s0], s->q[s2], false, 2));
     SDG_TRY(one_stage(s, 2, dt, s->q[s2], s->q[s0], s->q[s1], false, 2));
     s->cur = s1;
@@ -570,7 +574,7 @@ int sdg_solver_solve_host_pipelined(sdg_solver* s, int count, const double* cons
     for (int it = 0; it < nstep; it++) {
       const int s0 = cur, s1 = (cur + 1) % 3, s2 = (cur + 2) % 3;
       SDG_TRY(one_stage_on(s, 0, dt, io.q[s0], nullptr, io.q[s1], io.u, io.v, io.w, s->comp,
-                           false, 1));
+                           false, it == 0 ? 1 : 2));
       SDG_TRY(one_stage_on(s, 1, dt, io.q[s1], io.q[s0], io.q[s2], io.u, io.v, io.w, s->comp,
                            false, 2));
       SDG_TRY(one_stage_on(s, 2, dt, io.q[s2], io.q[s0], io.q[s1], io.u, io.v, io.w, s->comp,

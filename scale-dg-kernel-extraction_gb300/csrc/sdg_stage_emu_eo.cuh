@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS, emu_eo_min_blocks<P>())
   // Five FP64 operations a face node cost less than the two FP64 jumps, five
   // splits and two compensated products of the double-float form: that form
   // issued about a fifth of the kernel's instructions.  The velocity factors
-  // tP and tM come from fc_in when a stage before this one in the step
+  // tP and tM come from fc_in when an earlier stage of the same solver call
   // stored them.
   const double2* __restrict__ fcin = reinterpret_cast<const double2*>(a.fc_in);
   double2* __restrict__ fcout = reinterpret_cast<double2*>(a.fc_out);

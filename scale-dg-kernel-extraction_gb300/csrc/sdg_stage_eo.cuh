@@ -28,9 +28,9 @@
 //    qP (2VelP - 2α) - qM (2VelM - 2α) with 2α = |uP + uM| (the normal sign
 //    applied through the constant ±2): five FP64 operations per face node.
 //    Three of them form the velocity factors tP = ±2VelP - 2α and tM, which
-//    the three stages of a step share: the solver has its first stage store
-//    them (fc_out) and the other two read them (fc_in), two operations a face
-//    node there.
+//    every stage of one solver call shares (the velocity cannot change
+//    within a call): the call's first stage stores them (fc_out) and every
+//    later stage reads them (fc_in), two operations a face node there.
 //
 // Thread layout: phase 0 and the face flux run one thread per node / face
 // node as in stage_block; the three contraction phases run one thread per
