@@ -701,6 +701,32 @@ def bench_dropin_step(sdg, args, wl, fused_rate, opt=None):
             "scratch_bytes": nbytes}
 
 
+def bench_slabs(sdg, args, wl, fused_rate, nparts=4):
+    """The bench box split into z-slab partitions that exchange their face
+    planes before every stage (sdg_slabs_*): all partitions on this GPU, so
+    the rate shows the exchange's cost on one device (pack, one copy per
+    message, unpack), not multi-GPU scaling."""
+    p, ne = args.p, args.ne
+    s = sdg.Slabs(ne, ne, ne, p, wl["D"], wl["L"], nparts, opt=OPTS[args.opt],
+                  precision=PRECISIONS[args.precision])
+    s.upload(wl["q"], wl["u"], wl["v"], wl["w"])
+    s.step(wl["dt"], args.warmup)
+    sdg.synchronize()
+    k = max(2, min(args.steps, 20))
+    t0 = time.perf_counter()
+    s.step(wl["dt"], k)
+    sdg.synchronize()
+    t = time.perf_counter() - t0
+    rate = (p + 1) ** 3 * ne ** 3 * 3 * k / t / 1e9
+    out = {"workload": f"same {ne}^3 p={p} box as {nparts} z-slab partitions on one GPU, "
+                       "face planes exchanged before every stage",
+           "nparts": nparts, "gdof_updates_per_s": rate, "ms_per_step": 1e3 * t / k,
+           "steps": k, "exchange_bytes_per_stage": s.exchange_bytes(),
+           "ratio_to_single_box": rate / fused_rate}
+    s.close()
+    return out
+
+
 def bench_serving(sdg, args, rate=None, plain_cache=None):
     """Poisson arrivals of solves (Ne per axis U{4..32}, p U{2..11}, nstep
     U{10..500}, Gaussian tracer in a constant velocity, FP32 compute / FP64
@@ -980,6 +1006,8 @@ def run_ours(args, ws, rank, local):
         emit_section("dropin_step", bench_dropin_step(sdg, args, wl, value), sections)
         emit_section("dropin_step_opt1", bench_dropin_step(sdg, args, wl, value, sdg.OPT_OPT1),
                      sections)
+    if ws == 1 and not args.no_slabs:
+        emit_section("slabs", bench_slabs(sdg, args, wl, value), sections)
     if ws == 1 and not args.no_operators:
         emit_section("operators", bench_operators(sdg, args, peaks), sections)
     if ws == 1 and not args.no_ensemble:
@@ -1032,6 +1060,8 @@ def main() -> int:
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-dropin", action="store_true",
                     help="skip the per-stage drop-in path measurement")
+    ap.add_argument("--no-slabs", action="store_true",
+                    help="skip the z-slab partition measurement")
     ap.add_argument("--no-operators", action="store_true",
                     help="skip the standalone operator entry points (divlike, gradlike, "
                          "var5, matvec, Lift, update_halo, mesh build)")

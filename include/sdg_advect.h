@@ -396,6 +396,37 @@ int sdg_solver_launches_per_step(const sdg_solver* s);
 void* sdg_solver_stream(const sdg_solver* s);
 int sdg_solver_destroy(sdg_solver* s);
 
+/* ---- z-slab partitions with a face exchange per stage --------------------
+ * The halo exchange that update_halo (mod_mesh.f90:209-221) stands in for
+ * in the single-process reference, and that MPI carried in SCALE-DG
+ * (README.md:17): the box is split along z into nparts slabs of whole
+ * element layers, each partition keeps its owned layers plus one ghost
+ * layer on each side, and before every RK stage each partition sends the
+ * face plane its neighbours read (bottom owned layer, k = 0 nodes, to the
+ * partition below; top owned layer, k = Nq-1 nodes, to the one above,
+ * periodically) into the receiver's own ghost layer.  The partitions of one
+ * handle live on the current GPU and a message is a device-to-device copy;
+ * the plan and the packed buffers are those a multi-GPU run would send
+ * between ranks.  Results equal sdg_solver's on the whole box bit for bit. */
+typedef struct sdg_slabs sdg_slabs;
+/* The split: partition k owns layers [z_begin[k], z_begin[k+1]) (nparts+1
+ * entries, as even as possible); its lower ghost layer is filled by
+ * partition lo_src[k], its upper one by hi_src[k].  1 <= nparts <= NeZ.
+ * Host-only arithmetic. */
+int sdg_slab_plan(int NeZ, int nparts, int* z_begin, int* lo_src, int* hi_src);
+int sdg_slabs_create(sdg_slabs** out, int NeX, int NeY, int NeZ, int p,
+                     double Lx, double Ly, double Lz, const double* D1D,
+                     const double* Lift_mat, int opt, int precision, int nparts,
+                     void* stream);
+/* Host arrays of the whole box (Np*Ne each), as sdg_solver_upload. */
+int sdg_slabs_upload(sdg_slabs* s, const double* q, const double* u,
+                     const double* v, const double* w);
+int sdg_slabs_step(sdg_slabs* s, double dt, int nstep);
+int sdg_slabs_download(sdg_slabs* s, double* q);
+/* Bytes every partition together sends per RK stage. */
+long long sdg_slabs_exchange_bytes(const sdg_slabs* s);
+int sdg_slabs_destroy(sdg_slabs* s);
+
 /* ---- batched ensembles: one launch per RK stage and order --------------- */
 
 /* Many independent periodic boxes (orders 1..11, any sizes, each with its own

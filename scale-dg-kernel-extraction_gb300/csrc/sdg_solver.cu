@@ -41,6 +41,10 @@ struct sdg_solver {
   // Measured on GB300 against forming them in every stage: 1.04-1.13x for the
   // FP64 stage (p = 7: 19.3 against 18.5 GDOF-updates/s), 1.01-1.14x emulated.
   double* fc = nullptr;
+  // elements a stage advances: [elem_begin, elem_begin + elem_count) of the
+  // box (the whole box by default; a z-slab partition advances its owned
+  // layers and keeps a ghost layer on each side)
+  long long elem_begin = 0, elem_count = -1;
   // pipelined host-to-host solves (allocated on first use)
   IoSlot io[2];
   bool io_ready = false;
@@ -112,8 +116,8 @@ int one_stage_on(sdg_solver* s, int stage, double dt, const double* qin, const d
   a.D = s->D;
   a.Lift = s->Lift;
   a.box = s->box;
-  a.elem_begin = 0;
-  a.elem_count = s->box.Ne;
+  a.elem_begin = s->elem_begin;
+  a.elem_count = s->elem_count >= 0 ? s->elem_count : s->box.Ne;
   a.a = rk_a[stage];
   a.b = rk_b[stage];
   a.dt = dt;
@@ -234,29 +238,10 @@ void emu_eo_tables(int Nq, const Box& box, const double* D1D, const std::vector<
   std::memcpy(out.data(), f.data(), out.size());
 }
 
-}  // namespace
-
-extern "C" {
-
-int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
-                      double Lx, double Ly, double Lz, const double* D1D,
-                      const double* Lift_mat, int opt, int precision,
-                      void* stream) {
-  if (!out) return fail(SDG_ERR_INVALID_ARG, "NULL output handle");
-  *out = nullptr;
-  if (p < 1 || p > kMaxOrder)
-    return fail(SDG_ERR_UNSUPPORTED_ORDER, "PolyOrder %d outside 1..15", p);
-  if (NeX < 1 || NeY < 1 || NeZ < 1 || !(Lx > 0) || !(Ly > 0) || !(Lz > 0))
-    return fail(SDG_ERR_INVALID_ARG, "bad box %dx%dx%d (%g,%g,%g)", NeX, NeY, NeZ,
-                Lx, Ly, Lz);
-  if ((long long)NeX * NeY * NeZ > 0x7fffffffLL)
-    return fail(SDG_ERR_INVALID_ARG, "too many elements");
-  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1 && opt != SDG_OPT_EVENODD)
-    return fail(SDG_ERR_BAD_OPTTYPE, "unknown DGOptrKernel type %d", opt);
-  if (precision != SDG_PREC_FP64 && precision != SDG_PREC_FP32 &&
-      precision != SDG_PREC_FP64_EMU)
-    return fail(SDG_ERR_INVALID_ARG, "unknown precision %d", precision);
-  if (!D1D || !Lift_mat) return fail(SDG_ERR_INVALID_ARG, "NULL operator");
+// A solver on a given box (sizes and scale factors already checked): the
+// operator tables, the state, velocity and face-factor buffers.
+int solver_create_box(sdg_solver** out, const Box& box, int p, const double* D1D,
+                      const double* Lift_mat, int opt, int precision, void* stream) {
   SDG_TRY(require_device());
   sdg_solver* s = new (std::nothrow) sdg_solver();
   if (!s) return fail(SDG_ERR_OUT_OF_MEMORY, "host allocation failed");
@@ -265,7 +250,7 @@ int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
   s->Np = s->Nq * s->Nq * s->Nq;
   s->opt = opt;
   s->prec = precision;
-  s->box = make_box(NeX, NeY, NeZ, Lx, Ly, Lz);
+  s->box = box;
   s->ndof = (long long)s->Np * s->box.Ne;
   s->stream = as_stream(stream);
   // velocity element size: FP64 (FP64 and emulated forms) or FP32
@@ -316,6 +301,33 @@ int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
   }
   *out = s;
   return SDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdg_solver_create(sdg_solver** out, int NeX, int NeY, int NeZ, int p,
+                      double Lx, double Ly, double Lz, const double* D1D,
+                      const double* Lift_mat, int opt, int precision,
+                      void* stream) {
+  if (!out) return fail(SDG_ERR_INVALID_ARG, "NULL output handle");
+  *out = nullptr;
+  if (p < 1 || p > kMaxOrder)
+    return fail(SDG_ERR_UNSUPPORTED_ORDER, "PolyOrder %d outside 1..15", p);
+  if (NeX < 1 || NeY < 1 || NeZ < 1 || !(Lx > 0) || !(Ly > 0) || !(Lz > 0))
+    return fail(SDG_ERR_INVALID_ARG, "bad box %dx%dx%d (%g,%g,%g)", NeX, NeY, NeZ,
+                Lx, Ly, Lz);
+  if ((long long)NeX * NeY * NeZ > 0x7fffffffLL)
+    return fail(SDG_ERR_INVALID_ARG, "too many elements");
+  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1 && opt != SDG_OPT_EVENODD)
+    return fail(SDG_ERR_BAD_OPTTYPE, "unknown DGOptrKernel type %d", opt);
+  if (precision != SDG_PREC_FP64 && precision != SDG_PREC_FP32 &&
+      precision != SDG_PREC_FP64_EMU)
+    return fail(SDG_ERR_INVALID_ARG, "unknown precision %d", precision);
+  if (!D1D || !Lift_mat) return fail(SDG_ERR_INVALID_ARG, "NULL operator");
+  return solver_create_box(out, make_box(NeX, NeY, NeZ, Lx, Ly, Lz), p, D1D, Lift_mat, opt,
+                           precision, stream);
 }
 
 int sdg_solver_check_mesh(const sdg_solver* s, const int* VMapM, const int* VMapP,
@@ -609,6 +621,250 @@ void* sdg_solver_stream(const sdg_solver* s) { return s ? (void*)s->stream : nul
 int sdg_solver_destroy(sdg_solver* s) {
   if (!s) return SDG_OK;
   release(s);
+  delete s;
+  return SDG_OK;
+}
+
+}  // extern "C"
+
+// ---- z-slab partitions with a face exchange per stage -----------------------
+//
+// The box is split along z into nparts slabs of whole element layers.  Each
+// partition is a solver on its own extended box: its owned layers plus one
+// ghost layer below and one above, with the full box's scale factors.  Its
+// stages advance only the owned layers; an owned element's -z / +z
+// neighbour in the bottom / top layer is then the ghost element, reached
+// without the periodic wrap.  Before every stage the partitions exchange the
+// face planes the neighbour gathers read -- the bottom owned layer's k = 0
+// plane goes to the partition below, the top owned layer's k = Nq-1 plane to
+// the one above (periodically) -- through per-partition send and receive
+// buffers: pack on the sender, one copy per message, unpack into the
+// receiver's own ghost layer.  This is the exchange that update_halo
+// (mod_mesh.f90:209-221) stands in for in the single-process reference and
+// that MPI carried in SCALE-DG; here the partitions share one GPU, so a
+// message is a device-to-device copy (between GPUs it would be a peer copy or
+// an NCCL send / receive of the same buffers).  Every owned node computes
+// with the same values and factors as in the whole box, so the result equals
+// the single-box solver's bit for bit.
+
+struct sdg_slabs {
+  int nparts = 0, NeX = 0, NeY = 0, NeZ = 0, Nq = 0, Np = 0;
+  std::vector<int> z_begin, lo_src, hi_src;
+  std::vector<sdg_solver*> part;
+  double* planes = nullptr;  // per partition: send_lo, send_hi, recv_lo, recv_hi
+  long long plane_n = 0;     // doubles of one plane: NeX*NeY*Nq^2
+  cudaStream_t stream = nullptr;
+};
+
+namespace {
+
+// send_lo <- the k = 0 plane of the bottom owned layer (first element lo0);
+// send_hi <- the k = Nq-1 plane of the top owned layer (first element hi0).
+__global__ void slab_pack_kernel(const double* __restrict__ q, double* send_lo, double* send_hi,
+                                 long long lo0, long long hi0, long long n, int Nq) {
+  const int nq2 = Nq * Nq;
+  const long long np = (long long)nq2 * Nq;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long e = t / nq2;
+    const int n2 = (int)(t - e * nq2);
+    send_lo[t] = q[(lo0 + e) * np + n2];
+    send_hi[t] = q[(hi0 + e) * np + (long long)(Nq - 1) * nq2 + n2];
+  }
+}
+
+// The lower ghost layer (first element g_lo) receives the k = Nq-1 plane its
+// upper neighbour reads; the upper ghost layer (g_hi) the k = 0 plane.
+__global__ void slab_unpack_kernel(double* q, const double* __restrict__ recv_lo,
+                                   const double* __restrict__ recv_hi, long long g_lo,
+                                   long long g_hi, long long n, int Nq) {
+  const int nq2 = Nq * Nq;
+  const long long np = (long long)nq2 * Nq;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long e = t / nq2;
+    const int n2 = (int)(t - e * nq2);
+    q[(g_lo + e) * np + (long long)(Nq - 1) * nq2 + n2] = recv_lo[t];
+    q[(g_hi + e) * np + n2] = recv_hi[t];
+  }
+}
+
+int slab_layers(const sdg_slabs* s, int k) { return s->z_begin[k + 1] - s->z_begin[k]; }
+
+// The exchange before a stage reads state buffer `buf` of every partition.
+int slab_exchange(sdg_slabs* s, int buf) {
+  const long long nxy = (long long)s->NeX * s->NeY, n = s->plane_n;
+  const int P = s->nparts;
+  auto plane = [&](int k, int which) { return s->planes + (4LL * k + which) * n; };
+  for (int k = 0; k < P; k++) {
+    slab_pack_kernel<<<grid_for(n), 256, 0, s->stream>>>(
+        s->part[k]->q[buf], plane(k, 0), plane(k, 1), nxy, nxy * slab_layers(s, k), n, s->Nq);
+    SDG_CUDA_TRY(cudaGetLastError());
+  }
+  // messages: partition k's lower ghost plane comes from lo_src[k]'s top
+  // layer, its upper one from hi_src[k]'s bottom layer
+  for (int k = 0; k < P; k++) {
+    SDG_CUDA_TRY(cudaMemcpyAsync(plane(k, 2), plane(s->lo_src[k], 1), 8 * n,
+                                 cudaMemcpyDeviceToDevice, s->stream));
+    SDG_CUDA_TRY(cudaMemcpyAsync(plane(k, 3), plane(s->hi_src[k], 0), 8 * n,
+                                 cudaMemcpyDeviceToDevice, s->stream));
+  }
+  for (int k = 0; k < P; k++) {
+    slab_unpack_kernel<<<grid_for(n), 256, 0, s->stream>>>(
+        s->part[k]->q[buf], plane(k, 2), plane(k, 3), 0, nxy * (slab_layers(s, k) + 1), n,
+        s->Nq);
+    SDG_CUDA_TRY(cudaGetLastError());
+  }
+  return SDG_OK;
+}
+
+// Gathers partition k's extended layers (one ghost layer each side, periodic
+// in z) of a whole-box host field.
+void slab_extend(const sdg_slabs* s, int k, const double* full, std::vector<double>& out) {
+  const long long lay = (long long)s->NeX * s->NeY * s->Np;
+  const int nz = slab_layers(s, k);
+  out.resize((size_t)(lay * (nz + 2)));
+  for (int l = 0; l < nz + 2; l++) {
+    const int z = ((s->z_begin[k] - 1 + l) % s->NeZ + s->NeZ) % s->NeZ;
+    std::memcpy(out.data() + l * lay, full + z * lay, 8 * (size_t)lay);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdg_slab_plan(int NeZ, int nparts, int* z_begin, int* lo_src, int* hi_src) {
+  if (NeZ < 1 || nparts < 1 || nparts > NeZ)
+    return fail(SDG_ERR_INVALID_ARG, "cannot split %d element layers into %d slabs", NeZ,
+                nparts);
+  if (!z_begin || !lo_src || !hi_src) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  for (int k = 0; k <= nparts; k++) z_begin[k] = (int)((long long)k * NeZ / nparts);
+  for (int k = 0; k < nparts; k++) {
+    lo_src[k] = (k + nparts - 1) % nparts;
+    hi_src[k] = (k + 1) % nparts;
+  }
+  return SDG_OK;
+}
+
+int sdg_slabs_create(sdg_slabs** out, int NeX, int NeY, int NeZ, int p, double Lx, double Ly,
+                     double Lz, const double* D1D, const double* Lift_mat, int opt,
+                     int precision, int nparts, void* stream) {
+  if (!out) return fail(SDG_ERR_INVALID_ARG, "NULL output handle");
+  *out = nullptr;
+  if (p < 1 || p > kMaxOrder)
+    return fail(SDG_ERR_UNSUPPORTED_ORDER, "PolyOrder %d outside 1..15", p);
+  if (NeX < 1 || NeY < 1 || NeZ < 1 || !(Lx > 0) || !(Ly > 0) || !(Lz > 0))
+    return fail(SDG_ERR_INVALID_ARG, "bad box %dx%dx%d", NeX, NeY, NeZ);
+  if ((long long)NeX * NeY * (NeZ + 2LL * nparts) > 0x7fffffffLL)
+    return fail(SDG_ERR_INVALID_ARG, "too many elements");
+  if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1 && opt != SDG_OPT_EVENODD)
+    return fail(SDG_ERR_BAD_OPTTYPE, "unknown DGOptrKernel type %d", opt);
+  if (precision != SDG_PREC_FP64 && precision != SDG_PREC_FP32 &&
+      precision != SDG_PREC_FP64_EMU)
+    return fail(SDG_ERR_INVALID_ARG, "unknown precision %d", precision);
+  if (!D1D || !Lift_mat) return fail(SDG_ERR_INVALID_ARG, "NULL operator");
+  sdg_slabs* s = new (std::nothrow) sdg_slabs();
+  if (!s) return fail(SDG_ERR_OUT_OF_MEMORY, "host allocation failed");
+  s->nparts = nparts;
+  s->NeX = NeX;
+  s->NeY = NeY;
+  s->NeZ = NeZ;
+  s->Nq = p + 1;
+  s->Np = s->Nq * s->Nq * s->Nq;
+  s->stream = as_stream(stream);
+  s->z_begin.resize(nparts + 1);
+  s->lo_src.resize(nparts);
+  s->hi_src.resize(nparts);
+  int st = sdg_slab_plan(NeZ, nparts, s->z_begin.data(), s->lo_src.data(), s->hi_src.data());
+  if (st != SDG_OK) {
+    delete s;
+    return st;
+  }
+  const Box full = make_box(NeX, NeY, NeZ, Lx, Ly, Lz);
+  const long long nxy = (long long)NeX * NeY;
+  for (int k = 0; k < nparts && st == SDG_OK; k++) {
+    Box b = full;  // the whole box's scale factors, bit for bit
+    b.NeZ = slab_layers(s, k) + 2;
+    b.Ne = nxy * b.NeZ;
+    sdg_solver* ps = nullptr;
+    st = solver_create_box(&ps, b, p, D1D, Lift_mat, opt, precision, stream);
+    if (st == SDG_OK) {
+      ps->elem_begin = nxy;
+      ps->elem_count = nxy * slab_layers(s, k);
+      s->part.push_back(ps);
+    }
+  }
+  s->plane_n = nxy * s->Nq * s->Nq;
+  if (st == SDG_OK) {
+    const cudaError_t e = cudaMalloc(&s->planes, 8 * 4 * (size_t)nparts * (size_t)s->plane_n);
+    if (e != cudaSuccess) st = cuda_fail(e, "slab planes", __FILE__, __LINE__);
+  }
+  if (st != SDG_OK) {
+    sdg_slabs_destroy(s);
+    return st;
+  }
+  *out = s;
+  return SDG_OK;
+}
+
+int sdg_slabs_upload(sdg_slabs* s, const double* q, const double* u, const double* v,
+                     const double* w) {
+  if (!s || !q || !u || !v || !w) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  std::vector<double> eq, eu, ev, ew;
+  for (int k = 0; k < s->nparts; k++) {
+    slab_extend(s, k, q, eq);
+    slab_extend(s, k, u, eu);
+    slab_extend(s, k, v, ev);
+    slab_extend(s, k, w, ew);
+    SDG_TRY(sdg_solver_upload(s->part[k], eq.data(), eu.data(), ev.data(), ew.data()));
+    // the host vectors are reused for the next partition: let the copies land
+    SDG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  }
+  return SDG_OK;
+}
+
+int sdg_slabs_step(sdg_slabs* s, double dt, int nstep) {
+  if (!s) return fail(SDG_ERR_INVALID_ARG, "NULL slabs");
+  if (nstep < 0) return fail(SDG_ERR_INVALID_ARG, "nstep < 0");
+  for (int it = 0; it < nstep; it++) {
+    const int s0 = s->part[0]->cur, s1 = (s0 + 1) % 3, s2 = (s0 + 2) % 3;
+    SDG_TRY(slab_exchange(s, s0));
+    for (sdg_solver* ps : s->part)
+      SDG_TRY(one_stage(ps, 0, dt, ps->q[s0], nullptr, ps->q[s1], false, it == 0 ? 1 : 2));
+    SDG_TRY(slab_exchange(s, s1));
+    for (sdg_solver* ps : s->part)
+      SDG_TRY(one_stage(ps, 1, dt, ps->q[s1], ps->q[s0], ps->q[s2], false, 2));
+    SDG_TRY(slab_exchange(s, s2));
+    for (sdg_solver* ps : s->part)
+      SDG_TRY(one_stage(ps, 2, dt, ps->q[s2], ps->q[s0], ps->q[s1], false, 2));
+    for (sdg_solver* ps : s->part) ps->cur = s1;
+  }
+  return SDG_OK;
+}
+
+int sdg_slabs_download(sdg_slabs* s, double* q) {
+  if (!s || !q) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
+  const long long lay = (long long)s->NeX * s->NeY * s->Np;
+  for (int k = 0; k < s->nparts; k++) {
+    const sdg_solver* ps = s->part[k];
+    SDG_CUDA_TRY(cudaMemcpyAsync(q + s->z_begin[k] * lay, ps->q[ps->cur] + lay,
+                                 8 * (size_t)(lay * slab_layers(s, k)), cudaMemcpyDeviceToHost,
+                                 s->stream));
+  }
+  SDG_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return SDG_OK;
+}
+
+long long sdg_slabs_exchange_bytes(const sdg_slabs* s) {
+  return s ? 8LL * 2 * s->nparts * s->plane_n : 0;
+}
+
+int sdg_slabs_destroy(sdg_slabs* s) {
+  if (!s) return SDG_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (sdg_solver* ps : s->part) sdg_solver_destroy(ps);
+  cudaFree(s->planes);
   delete s;
   return SDG_OK;
 }

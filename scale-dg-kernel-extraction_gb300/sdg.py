@@ -116,6 +116,14 @@ def _load() -> C.CDLL:
         "sdg_mesh_setup_dev": ([_i, _i, _i, _i, _d, _d, _d, _vp] + [_vp] * 7 + [_vp], _i),
         "sdg_rk_stage_dev": ([_vp, _vp, _vp, _i, _i, _i, _d, _vp], _i),
         "sdg_advect3d_eq_step_scratch_bytes": ([_i, _i], C.c_size_t),
+        "sdg_slab_plan": ([_i, _i, _ip, _ip, _ip], _i),
+        "sdg_slabs_create": ([C.POINTER(_vp), _i, _i, _i, _i, _d, _d, _d, _dp, _dp, _i, _i, _i,
+                              _vp], _i),
+        "sdg_slabs_upload": ([_vp, _vp, _vp, _vp, _vp], _i),
+        "sdg_slabs_step": ([_vp, _d, _i], _i),
+        "sdg_slabs_download": ([_vp, _vp], _i),
+        "sdg_slabs_exchange_bytes": ([_vp], C.c_longlong),
+        "sdg_slabs_destroy": ([_vp], _i),
         "sdg_advect3d_eq_step_dev": ([_vp] * 13 + [_i] * 6 + [_d, _i, _i, _vp, C.c_size_t,
                                                           _vp, _vp], _i),
         "sdg_solver_create": ([C.POINTER(_vp), _i, _i, _i, _i, _d, _d, _d, _dp, _dp, _i, _i,
@@ -410,6 +418,54 @@ class PinnedArray:
     def __del__(self):
         try:
             self.free()
+        except Exception:
+            pass
+
+
+def slab_plan(NeZ: int, nparts: int):
+    """(z_begin, lo_src, hi_src) of the z-slab split (sdg_slab_plan, host only)."""
+    zb = np.zeros(nparts + 1, dtype=np.int32)
+    lo = np.zeros(max(nparts, 1), dtype=np.int32)
+    hi = np.zeros(max(nparts, 1), dtype=np.int32)
+    _check(lib.sdg_slab_plan(NeZ, nparts, zb, lo, hi), "sdg_slab_plan")
+    return zb, lo[:nparts], hi[:nparts]
+
+
+class Slabs:
+    """The box split into z-slab partitions with a face exchange per stage
+    (sdg_slabs_* in include/sdg_advect.h)."""
+
+    def __init__(self, NeX, NeY, NeZ, p, D1D, Lift_mat, nparts, opt=OPT_OPT1,
+                 precision=PREC_FP64, L=(1.0, 1.0, 1.0), stream=None):
+        self._h = _vp()
+        self.ndof = (p + 1) ** 3 * NeX * NeY * NeZ
+        _check(lib.sdg_slabs_create(C.byref(self._h), NeX, NeY, NeZ, p, float(L[0]),
+                                    float(L[1]), float(L[2]), _f64(D1D), _f64(Lift_mat), opt,
+                                    precision, nparts, stream), "sdg_slabs_create")
+
+    def upload(self, q, u, v, w) -> None:
+        arrs = [_f64(x) for x in (q, u, v, w)]
+        _check(lib.sdg_slabs_upload(self._h, *[x.ctypes.data for x in arrs]), "sdg_slabs_upload")
+
+    def step(self, dt: float, nstep: int) -> None:
+        _check(lib.sdg_slabs_step(self._h, float(dt), int(nstep)), "sdg_slabs_step")
+
+    def download(self) -> np.ndarray:
+        out = np.zeros(self.ndof)
+        _check(lib.sdg_slabs_download(self._h, out.ctypes.data), "sdg_slabs_download")
+        return out
+
+    def exchange_bytes(self) -> int:
+        return int(lib.sdg_slabs_exchange_bytes(self._h))
+
+    def close(self) -> None:
+        if self._h is not None and self._h.value:
+            lib.sdg_slabs_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 
