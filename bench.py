@@ -727,6 +727,55 @@ def bench_slabs(sdg, args, wl, fused_rate, nparts=4):
     return out
 
 
+def bench_tensor_cores(sdg, args, reps=20):
+    """The FP32 contraction of tensorprod_divlike_dirXYZ (three directions)
+    at p = 15 on 16^3 elements (16.8M nodes, 201 MB of FP32 input and 201 MB
+    of output): on the tensor cores (tcgen05 kind::tf32, 3xTF32 pairs) and on
+    the CUDA cores, each queued `reps` times and timed on the host with a
+    synchronize on both sides, beside one FP32 even-odd stage of the same box
+    (the contractions are its dominant arithmetic)."""
+    import workloads as W
+    p, ne = 15, 16
+    nq = p + 1
+    ne3 = ne ** 3
+    n = nq ** 3 * ne3
+    x, D, Dt, L = W.reference_operators(p)
+    lib, A = sdg.lib, sdg.DeviceArray
+    rng = np.random.default_rng(args.seed + 9)
+    ins = [A(rng.standard_normal(n).astype(np.float32)) for _ in range(3)]
+    outs = [A(n=n, dtype=np.float32) for _ in range(3)]
+    Dd = A(np.asarray(D, dtype=np.float32))
+    err = A(np.zeros(1, dtype=np.int32))
+    res = {"workload": f"{ne}^3 elements at p = {p}, FP32 arrays, three directions, "
+                       f"{reps} queued calls each"}
+    for name, tc in (("tensor_cores", 1), ("cuda_cores", 0)):
+        def call():
+            sdg._check(lib.sdg_tensorprod_divlike_dirXYZ_f32_dev(
+                outs[0].ptr, outs[1].ptr, outs[2].ptr, Dd.ptr, ins[0].ptr, ins[1].ptr,
+                ins[2].ptr, nq, ne3, tc, err.ptr, None), "divlike_f32")
+        call()
+        sdg.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            call()
+        sdg.synchronize()
+        t = (time.perf_counter() - t0) / reps
+        res[name] = {"ms_per_call": 1e3 * t, "gbs": 24.0 * n / t / 1e9,
+                     "tflops": 2.0 * 3 * nq * n / t / 1e12}
+    assert int(err.numpy()[0]) == 0
+    q, u, v, w = W.blob(ne, ne, ne, x, args.seed + 15)
+    s = sdg.Solver(ne, ne, ne, p, D, L, opt=sdg.OPT_EVENODD, precision=sdg.PREC_FP32)
+    s.upload(q, u, v, w)
+    dt = W.cfl_dt(ne, ne, ne, p, u, v, w)
+    s.step(dt, 2)
+    ms = s.step_timed(dt, 10)
+    s.close()
+    res["fp32_evenodd_stage_ms"] = ms / 30.0
+    res["tensor_over_cuda_cores"] = (res["cuda_cores"]["ms_per_call"] /
+                                     res["tensor_cores"]["ms_per_call"])
+    return res
+
+
 def bench_serving(sdg, args, rate=None, plain_cache=None):
     """Poisson arrivals of solves (Ne per axis U{4..32}, p U{2..11}, nstep
     U{10..500}, Gaussian tracer in a constant velocity, FP32 compute / FP64
@@ -1010,6 +1059,7 @@ def run_ours(args, ws, rank, local):
         emit_section("slabs", bench_slabs(sdg, args, wl, value), sections)
     if ws == 1 and not args.no_operators:
         emit_section("operators", bench_operators(sdg, args, peaks), sections)
+        emit_section("tensor_core_contraction", bench_tensor_cores(sdg, args), sections)
     if ws == 1 and not args.no_ensemble:
         emit_section("ensemble", bench_ensemble(sdg, args), sections)
     if ws == 1 and not args.no_serving:

@@ -270,6 +270,21 @@ int sdg_tensorprod_Lift_hexahedral_dev(double* vec_out, const double* Lift,
                                        const double* vec_in, int Nq, int nelem,
                                        void* stream);
 
+/* tensorprod_divlike_dirXYZ (mod_dg_optr_kernel.f90:62-136) in FP32
+ * arithmetic over nelem elements of FP32 device arrays (D1D as FP32,
+ * column-major).  use_tensor_cores = 1 (Nq = 16, p = 15 only): the three
+ * directions as dense products on the tensor cores, lines of a direction
+ * batched along M (tcgen05.mma kind::tf32, M = 128, N = K = 16, operands
+ * split into TF32 pairs, hi*hi + hi*lo + lo*hi, FP32 accumulation); a wait
+ * that runs out sets *err_flag to 1.  use_tensor_cores = 0: the same FP32
+ * contraction on the CUDA cores (any Nq).  No summation order of the
+ * reference: the results are FP32 approximations of its FP64 ones. */
+int sdg_tensorprod_divlike_dirXYZ_f32_dev(float* out_x, float* out_y, float* out_z,
+                                          const float* D1D, const float* in_x,
+                                          const float* in_y, const float* in_z,
+                                          int Nq, int nelem, int use_tensor_cores,
+                                          int* err_flag, void* stream);
+
 /* update_halo (mod_mesh.f90:209-221) on a device field f(Np*NeA):
  * f(Np*Ne+b) = f(halo_src_map(b)), b = 1..NhaloNode (1-based map).  A map
  * entry outside the owned DOFs 1..Np*Ne (the only targets mesh_setup

@@ -117,6 +117,7 @@ def _load() -> C.CDLL:
         "sdg_rk_stage_dev": ([_vp, _vp, _vp, _i, _i, _i, _d, _vp], _i),
         "sdg_advect3d_eq_step_scratch_bytes": ([_i, _i], C.c_size_t),
         "sdg_slab_plan": ([_i, _i, _ip, _ip, _ip], _i),
+        "sdg_tensorprod_divlike_dirXYZ_f32_dev": ([_vp] * 7 + [_i, _i, _i, _vp, _vp], _i),
         "sdg_slabs_create": ([C.POINTER(_vp), _i, _i, _i, _i, _d, _d, _d, _dp, _dp, _i, _i, _i,
                               _vp], _i),
         "sdg_slabs_upload": ([_vp, _vp, _vp, _vp, _vp], _i),
@@ -318,6 +319,25 @@ def tensorprod_Lift_hexahedral(Lift, vec_in, Nq):
     _check(lib.sdg_tensorprod_Lift_hexahedral(out, _f64(Lift), vi, Nq, nelem),
            "tensorprod_Lift_hexahedral")
     return out
+
+
+def tensorprod_divlike_dirXYZ_f32(D1D, in_x, in_y, in_z, Nq, tensor_cores=True):
+    """FP32 divlike of len(in_x) // Nq^3 elements through
+    sdg_tensorprod_divlike_dirXYZ_f32_dev (tensor cores at Nq = 16, else the
+    CUDA-core form).  Returns (out_x, out_y, out_z) as float32 arrays."""
+    ins = [DeviceArray(np.ascontiguousarray(a, dtype=np.float32)) for a in (in_x, in_y, in_z)]
+    n = ins[0].n
+    nelem = n // Nq ** 3
+    outs = [DeviceArray(n=n, dtype=np.float32) for _ in range(3)]
+    Dd = DeviceArray(np.ascontiguousarray(D1D, dtype=np.float32))
+    err = DeviceArray(np.zeros(1, dtype=np.int32))
+    _check(lib.sdg_tensorprod_divlike_dirXYZ_f32_dev(
+        outs[0].ptr, outs[1].ptr, outs[2].ptr, Dd.ptr, ins[0].ptr, ins[1].ptr, ins[2].ptr, Nq,
+        nelem, 1 if tensor_cores else 0, err.ptr, None), "tensorprod_divlike_dirXYZ_f32")
+    if int(err.numpy()[0]):
+        raise SdgError(ERR_TIMEOUT, "tensorprod_divlike_dirXYZ_f32",
+                       "the tensor-core wait ran out")
+    return tuple(o.numpy() for o in outs)
 
 
 def advect3d_eq_step(q, u, v, w, D1D, D1D_tr, Lift_mat, VMapM, VMapP, normal_fn, Escale,
