@@ -193,6 +193,30 @@ __global__ void step_face_kernel(const int* __restrict__ VMapM, const int* __res
   }
 }
 
+// Once per call, one warp per element: whether the element's Escale is one
+// value per direction over all its nodes (compared bit for bit), stored as
+// (Es_x, Es_y, Es_z, 1), else (.., 0).
+__global__ void step_escale_kernel(const double* __restrict__ Es, double4* esu, long long Ne,
+                                   int Np) {
+  const long long NpNe = (long long)Np * Ne;
+  const int lane = threadIdx.x & 31;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long e = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; e < Ne;
+       e += nwarps) {
+    double v[3];
+    bool same = true;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const double* x = Es + e * Np + d * NpNe;
+      v[d] = x[0];
+      const long long b = __double_as_longlong(v[d]);
+      for (int n = lane; n < Np; n += 32) same &= (__double_as_longlong(x[n]) == b);
+    }
+    same = __all_sync(0xffffffffu, same);
+    if (lane == 0) esu[e] = make_double4(v[0], v[1], v[2], same ? 1.0 : 0.0);
+  }
+}
+
 unsigned grid_for(long long n) {
   long long nb = (n + 255) / 256;
   if (nb > 152LL * 64) nb = 152LL * 64;
@@ -512,15 +536,16 @@ int sdg_rk_stage_dev(double* q, const double* q0, const double* dqdt, int Np,
 
 // Scratch of sdg_advect3d_eq_step_dev, 256-byte aligned pieces: two stage
 // states (Np*Ne), the face factors (tP, tM) per face node, the resolved
-// gather indices (M, P) per face node, and the even-odd tables.
-static size_t step_layout(int Nq, long long Ne, size_t off[5]) {
+// gather indices (M, P) per face node, the even-odd tables, and per element
+// its Escale when that is one value per direction.
+static size_t step_layout(int Nq, long long Ne, size_t off[6]) {
   const long long np = (long long)Nq * Nq * Nq, nft = 6LL * Nq * Nq * Ne;
   const int N = Nq, H = N / 2, HR = (N + 1) / 2;
   const long long te = (long long)H * H + (long long)HR * H + (N & 1) * H + HR + H;
-  const size_t sizes[5] = {(size_t)(8 * np * Ne), (size_t)(8 * np * Ne), (size_t)(16 * nft),
-                           (size_t)(8 * nft), (size_t)(8 * 3 * te)};
+  const size_t sizes[6] = {(size_t)(8 * np * Ne), (size_t)(8 * np * Ne), (size_t)(16 * nft),
+                           (size_t)(8 * nft), (size_t)(8 * 3 * te), (size_t)(32 * Ne)};
   size_t total = 0;
-  for (int k = 0; k < 5; k++) {
+  for (int k = 0; k < 6; k++) {
     off[k] = total;
     total += (sizes[k] + 255) & ~size_t(255);
   }
@@ -529,7 +554,7 @@ static size_t step_layout(int Nq, long long Ne, size_t off[5]) {
 
 size_t sdg_advect3d_eq_step_scratch_bytes(int Nq, int Ne) {
   if (Nq - 1 < 1 || Nq - 1 > kMaxOrder || Ne < 0) return 0;
-  size_t off[5];
+  size_t off[6];
   return step_layout(Nq, Ne, off);
 }
 
@@ -551,7 +576,7 @@ int sdg_advect3d_eq_step_dev(double* q, const double* u, const double* v, const 
   if ((long long)Np * NeA > 0x7fffffffLL)
     return fail(SDG_ERR_INVALID_ARG, "Np*NeA beyond the 32-bit DOF ids of VMapM/VMapP");
   if (Ne == 0 || nstep == 0) return SDG_OK;
-  size_t off[5];
+  size_t off[6];
   const size_t need = step_layout(Nq, Ne, off);
   if (!scratch || scratch_bytes < need)
     return fail(SDG_ERR_INVALID_ARG, "scratch of %zu bytes, %zu needed "
@@ -602,13 +627,17 @@ int sdg_advect3d_eq_step_dev(double* q, const double* u, const double* v, const 
   double2* fc = reinterpret_cast<double2*>(base + off[2]);
   int2* res = reinterpret_cast<int2*>(base + off[3]);
   double* tab = reinterpret_cast<double*>(base + off[4]);
+  double4* esu = reinterpret_cast<double4*>(base + off[5]);
   StepTablesArgs tb{D1D, D1D_tr, Lift_mat, tab, err_flag};
   SDG_TRY(dropin(p, 5, opt, &tb, st));
   step_face_kernel<<<grid_for(nft), 256, 0, st>>>(VMapM, VMapP, halo_src_map, u, v, w,
                                                   normal_fn, Fscale, res, fc, nft, npne,
                                                   np * NeA, NhaloNode, err_flag);
   SDG_CUDA_TRY(cudaGetLastError());
+  step_escale_kernel<<<grid_for(32LL * Ne), 256, 0, st>>>(Escale, esu, Ne, Np);
+  SDG_CUDA_TRY(cudaGetLastError());
   StepRefArgs a{};
+  a.esu = esu;
   a.u = u;
   a.v = v;
   a.w = w;

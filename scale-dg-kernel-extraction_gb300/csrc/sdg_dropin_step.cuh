@@ -21,7 +21,12 @@
 //     step_face_kernel forms them once per call and every stage reads them;
 //   * Escale (per node, per direction): applied to each direction's
 //     derivative sum before the lift is added, as cal_dqdt does
-//     (mod_advect3d_eq.f90:185-198).
+//     (mod_advect3d_eq.f90:185-198).  Where an element's Escale is one value
+//     per direction (mesh_setup's affine elements, mod_mesh.f90:147-149;
+//     step_escale_kernel checks every node once per call) the value is
+//     folded into that element's copy of the derivative tables instead, and
+//     its lines run the structured stage's body (eo_line); elements with
+//     Escale varying node by node keep the per-node form (eo_line_esc).
 // The summation order is the even-odd one of dqdt_eo_kernel: neither
 // GENERAL's nor OPT1's, equal to both to rounding.
 #pragma once
@@ -43,6 +48,8 @@ struct StepRefArgs {
                         //   from (-1: a map entry was out of range)
   const double2* fc;    // per face node: the velocity factors (tP, tM)
   const double* Escale;
+  const double4* esu;   // per element: (Es_x, Es_y, Es_z, 1) when its Escale is
+                        //   one value per direction, (.., 0) otherwise
   int Ne;
   double a, b, c;       // q_out = a q0 + b q_in + c S, c = -b dt, S = -dqdt
                         // (the tables are scaled by c)
@@ -59,7 +66,7 @@ template <int P>
 constexpr size_t step_ref_smem_bytes() {
   using O = Ord<P>;
   return sizeof(double) * (size_t)(3 * EoShape<P>::TE +
-                                   StepRefCfg<P>::EPB * (O::NP + O::NFT));
+                                   StepRefCfg<P>::EPB * (O::NP + O::NFT + 3 * EoShape<P>::TE));
 }
 
 // The three directions' unscaled even-odd tables from D1D and Lift_mat (the
@@ -195,12 +202,21 @@ __global__ void __launch_bounds__(StepRefCfg<P>::THREADS, 4) step_ref_kernel(con
   double* sT = reinterpret_cast<double*>(smem_raw);  // [3][TE]
   double* sA = sT + 3 * TE;                          // [EPB][NP]: x pairs, then sums
   double* sf = sA + EPB * NP;                        // [EPB][NFT] face fluxes
+  double* sTe = sf + EPB * NFT;                      // [EPB][3][TE] per element
   const long long eb = (long long)blockIdx.x * EPB;
   const int nloc = (int)min((long long)EPB, (long long)a.Ne - eb);
   if (nloc <= 0) return;
   // the tables times the stage factor c = -b dt: the line results are then
-  // the stage's increments, and the RK update needs no multiply of its own
+  // the stage's increments, and the RK update needs no multiply of its own;
+  // an element with one Escale per direction gets its own copy with the
+  // derivative parts also times Es_d
   for (int t = threadIdx.x; t < 3 * TE; t += T) sT[t] = a.tab[t] * a.c;
+  for (int t = threadIdx.x; t < nloc * 3 * TE; t += T) {
+    const int le = t / (3 * TE), w3 = t - le * 3 * TE, dir = w3 / TE, w = w3 - dir * TE;
+    const double4 es = a.esu[eb + le];
+    const double sd = (dir == 0) ? es.x : (dir == 1) ? es.y : es.z;
+    sTe[t] = (w < Sh::OFF_A) ? a.tab[w3] * (a.c * sd) : a.tab[w3] * a.c;
+  }
   const long long g0 = eb * NP;
   const double* __restrict__ q = a.q_in;
   const double* __restrict__ gu = a.u;
@@ -232,12 +248,18 @@ __global__ void __launch_bounds__(StepRefCfg<P>::THREADS, 4) step_ref_kernel(con
   const int r = threadIdx.x % NQ2, le = threadIdx.x / NQ2;
   const bool has_line = threadIdx.x < nloc * NQ2;
   const double* fl = sf + le * NFT + r;
+  // one Escale per direction for this line's element: the folded tables
+  const bool uni = has_line && a.esu[eb + le].w != 0.0;
+  const double* Te = sTe + le * 3 * TE;
   // x lines: faces -x (3) and +x (1); Escale_x D F + lift over the pair values
   if (has_line) {
     double* row = sA + le * NP + r * NQ;
     const long long g = g0 + (long long)le * NP + (long long)r * NQ;
-    eo_line_esc<P>(row, sT, fl[3 * NFP], fl[1 * NFP], [&](int m) { return Es[g + m]; },
-                   [&](int m, double r) { row[m] = r; });
+    auto emit = [&](int m, double r) { row[m] = r; };
+    if (uni)
+      eo_line<P, 1, 1, true>(row, Te, fl[3 * NFP], fl[1 * NFP], 0, emit);
+    else
+      eo_line_esc<P>(row, sT, fl[3 * NFP], fl[1 * NFP], [&](int m) { return Es[g + m]; }, emit);
   }
   __syncthreads();
   // y lines: faces -y (0) and +y (2); added into the sums
@@ -245,9 +267,12 @@ __global__ void __launch_bounds__(StepRefCfg<P>::THREADS, 4) step_ref_kernel(con
     const int off = le * NP + (r % NQ) + (r / NQ) * NQ2;
     double row[NQ];
     eo_pairs_f64<P>(q, a.v, g0 + off, NQ, row);
-    eo_line_esc<P>(row, sT + TE, fl[0], fl[2 * NFP],
-                   [&](int m) { return Es[g0 + off + m * NQ + NpNe]; },
-                   [&](int m, double r) { sA[off + m * NQ] += r; });
+    auto emit = [&](int m, double r) { sA[off + m * NQ] += r; };
+    if (uni)
+      eo_line<P, 1, 1, true>(row, Te + TE, fl[0], fl[2 * NFP], 0, emit);
+    else
+      eo_line_esc<P>(row, sT + TE, fl[0], fl[2 * NFP],
+                     [&](int m) { return Es[g0 + off + m * NQ + NpNe]; }, emit);
   }
   __syncthreads();
   // z lines: faces -z (4) and +z (5); finish the node and the RK update
@@ -258,17 +283,18 @@ __global__ void __launch_bounds__(StepRefCfg<P>::THREADS, 4) step_ref_kernel(con
     double* __restrict__ qout = a.q_out;
     const double* q0 = a.q0;
     const double ra = a.a, rb = a.b;
-    eo_line_esc<P>(row, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP],
-                   [&](int m) { return Es[g0 + off + m * NQ2 + 2 * NpNe]; },
-                   [&](int m, double r) {
-                     const int n = off + m * NQ2;
-                     const long long g = g0 + n;
-                     // q0 is read before q_out is written at the same node,
-                     // by this thread only, so the third stage may write the
-                     // result over q0
-                     qout[g] = rk_combine<RK>(sA[n] + r, q[g],
-                                              RK == kRkGeneral ? q0[g] : 0.0, ra, rb);
-                   });
+    auto emit = [&](int m, double r) {
+      const int n = off + m * NQ2;
+      const long long g = g0 + n;
+      // q0 is read before q_out is written at the same node, by this thread
+      // only, so the third stage may write the result over q0
+      qout[g] = rk_combine<RK>(sA[n] + r, q[g], RK == kRkGeneral ? q0[g] : 0.0, ra, rb);
+    };
+    if (uni)
+      eo_line<P, 1, 1, true>(row, Te + 2 * TE, fl[4 * NFP], fl[5 * NFP], 0, emit);
+    else
+      eo_line_esc<P>(row, sT + 2 * TE, fl[4 * NFP], fl[5 * NFP],
+                     [&](int m) { return Es[g0 + off + m * NQ2 + 2 * NpNe]; }, emit);
   }
 }
 

@@ -794,3 +794,27 @@ def test_reference_array_step_reports_bad_maps_and_scratch():
                                           m.NeA, m.NhaloNode, c.dt, 1, sdg.OPT_EVENODD,
                                           small.ptr, need // 2, qd.ptr, None)
     assert st == sdg.ERR_INVALID_ARG
+
+
+def test_reference_array_step_mixes_folded_and_per_node_escale():
+    """Elements whose Escale is one value per direction (here a different
+    value for each element) run with Escale folded into their tables, the
+    others node by node; both kinds side by side in one call, against the
+    oracle's loop on the same arrays."""
+    import copy
+    c = Case(3, 2, 3, 5, ic="blob")
+    m = copy.copy(c.mesh)
+    rng = np.random.default_rng(321)
+    Es = c.mesh.Escale.reshape(3, m.Ne, m.Np).copy()
+    for e in range(m.Ne):
+        if e % 2 == 0:
+            Es[:, e, :] *= (1.0 + 0.05 * e)  # uniform per direction, element's own value
+        else:
+            Es[:, e, :] *= 1.0 + 0.2 * rng.random((3, m.Np))  # node by node
+    m.Escale = Es.reshape(-1)
+    for opt in (sdg.OPT_EVENODD, sdg.OPT_OPT1):
+        q = sdg.advect3d_eq_step(c.q, c.u, c.v, c.w, c.D, c.Dt, c.Lift, *_step_args(c, m), c.dt,
+                                 4, opt)
+        qq = c.q.copy()
+        O.run(m, qq, c.u, c.v, c.w, c.D, c.Dt, c.Lift, c.dt, 4, O.OPT1)
+        assert rel_l2(q[: c.nown], qq[: c.nown]) <= TOL_RUN
