@@ -70,9 +70,12 @@ struct EoShape {
 // a line measured faster on GB300 up to p = 3 in the single-box kernel (p = 3:
 // 91.8 against 72.5 GDOF-updates/s).  The FP64 body is bound by the FP64 pipe
 // and keeps one.  The batched kernels pick their own count (batch_eo_parts).
+// At p = 4 and 6 one thread a line measured faster (77.5 against 70.0
+// GDOF-updates/s at p = 4 with 256 threads and six blocks an SM; 77.3 against
+// 69.1 at p = 6 with four), at p = 5 slower (78.2 against 80.0).
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_parts() {
-  return (sizeof(CT) == 4 && P >= 4) ? 2 : 1;
+  return (sizeof(CT) == 4 && P >= 4 && P != 4 && P != 6) ? 2 : 1;
 }
 
 // Lines of a block: 256, or 128 for the FP32 body at p = 7, 9 and 10, where
@@ -458,6 +461,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_min_blocks() {
   if (sizeof(CT) == 8) return (P == 5 || P == 7 || P >= 14) ? 4 : 5;
+  if (P == 4) return 6;  // 40 registers, one thread a line (above)
   return (P <= 3 || P == 5 || eo_lines<P, CT>() == 128) ? 8 : P <= 12 ? 4 : 3;
 }
 
