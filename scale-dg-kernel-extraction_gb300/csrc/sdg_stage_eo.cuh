@@ -328,11 +328,28 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   // before this one in the step stored them (FP64 body).
   const double2* __restrict__ fcin = reinterpret_cast<const double2*>(a.fc_in);
   double2* __restrict__ fcout = reinterpret_cast<double2*>(a.fc_out);
+  // Below p = 5 a face has fewer nodes than a warp has lanes: the tasks go
+  // face-major there (all elements' nodes of face 0, then face 1, ...), so
+  // that the face -- and the branch on it in face_nodes -- is the same for
+  // all lanes of a warp but at a face boundary.  f = t / (nloc*NFP) by a
+  // multiply-high with ceil(2^32 / W), exact for t*W < 2^32.
+  const unsigned fW = (unsigned)(nloc * NFP);
+  const unsigned fmagic = 0xFFFFFFFFu / fW + 1u;
   for (int t = threadIdx.x; t < nloc * NFT; t += T) {
-    const int le = t / NFT;
-    const int r = t - le * NFT;
-    const int f = r / NFP;
-    const int fp = r - f * NFP;
+    int le, f, fp;
+    if constexpr (NFP < 32) {
+      f = (int)__umulhi((unsigned)t, fmagic);
+      const int rem = t - f * (int)fW;
+      le = rem / NFP;
+      fp = rem - le * NFP;
+    } else {
+      le = t / NFT;
+      const int rr = t - le * NFT;
+      f = rr / NFP;
+      fp = rr - f * NFP;
+    }
+    const int r = f * NFP + fp;
+    const int ti = le * NFT + r;  // the task's element-major index
     int nM, nP, axis, sg;
     face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sg);
     const long long gM = g0 + (long long)le * NP + nM;
@@ -345,7 +362,7 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
     const CT qP = to_ct<CT>(qin[gP]);
     CT tP, tM;
     if (kF64 && fcin != nullptr) {
-      const double2 c = fcin[eb * NFT + t];
+      const double2 c = fcin[eb * NFT + ti];
       tP = CT(c.x);
       tM = CT(c.y);
     } else {
@@ -355,9 +372,9 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
       const CT tw = (sg > 0) ? CT(2) : CT(-2);
       tP = fma(tw, uP, -a2);
       tM = fma(tw, uM, -a2);
-      if (kF64 && fcout != nullptr) fcout[eb * NFT + t] = make_double2(tP, tM);
+      if (kF64 && fcout != nullptr) fcout[eb * NFT + ti] = make_double2(tP, tM);
     }
-    sf[le * NFT + r] = fma(qP, tP, -(qM * tM));
+    sf[ti] = fma(qP, tP, -(qM * tM));
   }
   __syncthreads();
 
