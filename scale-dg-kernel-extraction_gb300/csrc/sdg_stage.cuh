@@ -146,6 +146,36 @@ __device__ __forceinline__ void face_nodes(int f, int ta, int tb, int& nM,
   }
 }
 
+// Face-flux task t (t < nloc * 6 Nq^2) of a block with nloc elements ->
+// element le, face f, face node fp.  Below p = 5 a face has fewer nodes than
+// a warp has lanes, and tasks taken element by element mix two to four faces
+// in a warp, each lane on its own branch of face_nodes; there the tasks go
+// face-major (every element's nodes of face 0, then face 1, ...), which keeps
+// the face uniform across a warp but at face boundaries.  The face is found
+// by a multiply-high with ceil(2^32 / W), W = nloc Nq^2, exact for t W < 2^32.
+// The task's element-major index le * 6 Nq^2 + f Nq^2 + fp is what the face
+// arrays are indexed by in either order.
+template <int NQ>
+struct FaceTasks {
+  static constexpr int NFP = NQ * NQ, NFT = 6 * NFP;
+  unsigned W, magic;
+  __device__ __forceinline__ explicit FaceTasks(int nloc)
+      : W((unsigned)(nloc * NFP)), magic(0xFFFFFFFFu / (unsigned)(nloc * NFP) + 1u) {}
+  __device__ __forceinline__ void map(int t, int& le, int& f, int& fp) const {
+    if constexpr (NFP < 32) {
+      f = (int)__umulhi((unsigned)t, magic);
+      const int rem = t - f * (int)W;
+      le = rem / NFP;
+      fp = rem - le * NFP;
+    } else {
+      le = t / NFT;
+      const int r = t - le * NFT;
+      f = r / NFP;
+      fp = r - f * NFP;
+    }
+  }
+};
+
 // Neighbour across face f with periodic wrap (eval_neighbor_element,
 // mod_mesh.f90:407-483); element index e = ex + ey*NeX + ez*NeX*NeY.  The
 // element count is below 2^31 (checked at creation), so the index arithmetic
@@ -240,11 +270,11 @@ __device__ __forceinline__ void stage_block(const StageArgs& a, long long eb, in
     hfy = 0.5 * a.box.Fs[1];
     hfz = 0.5 * a.box.Fs[2];
   }
+  const FaceTasks<NQ> ftask(nloc);
   for (int t = threadIdx.x; t < nloc * NFT; t += T) {
-    const int le = t / NFT;
-    const int r = t - le * NFT;
-    const int f = r / NFP;
-    const int fp = r - f * NFP;
+    int le, f, fp;
+    ftask.map(t, le, f, fp);
+    const int r = f * NFP + fp;
     int nM, nP, axis, sg;
     face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sg);
     const long long gM = g0 + (long long)le * NP + nM;

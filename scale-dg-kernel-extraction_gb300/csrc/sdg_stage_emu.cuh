@@ -116,11 +116,11 @@ __global__ void __launch_bounds__(EmuCfg<P>::THREADS) stage_emu_kernel(const Sta
   __syncthreads();
 
   // phase 1a: upwind face fluxes g = qP (VP - VM) + (qP - qM)(VM - alpha)
+  const FaceTasks<NQ> ftask(nloc);  // face-major below p = 5
   for (int t = threadIdx.x; t < nloc * NFT; t += T) {
-    const int le = t / NFT;
-    const int r = t - le * NFT;
-    const int f = r / NFP;
-    const int fp = r - f * NFP;
+    int le, f, fp;
+    ftask.map(t, le, f, fp);
+    const int ti = le * NFT + f * NFP + fp;  // element-major index of the task
     int nM, nP, axis, sgi;
     face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sgi);
     const long long gM = g0 + (long long)le * NP + nM;
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(EmuCfg<P>::THREADS) stage_emu_kernel(const Sta
     dacc_fma(A, df_split(qP), df_split(jV));
     dacc_fma(A, df_split(jq), df_sub(dVM, alpha));
     const dfl gf = dacc_result(A);
-    sg[t] = make_float2(gf.hi, gf.lo);
+    sg[ti] = make_float2(gf.hi, gf.lo);
   }
   // phase 1b: G = q u_d - F0 (one FMA), split to double-float into the planes
   for (int t = threadIdx.x; t < nloc * NP; t += T) {

@@ -223,11 +223,11 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS, emu_eo_min_blocks<P>())
   // stored them.
   const double2* __restrict__ fcin = reinterpret_cast<const double2*>(a.fc_in);
   double2* __restrict__ fcout = reinterpret_cast<double2*>(a.fc_out);
+  const FaceTasks<NQ> ftask(nloc);  // face-major below p = 5
   for (int t = threadIdx.x; t < nloc * NFT; t += T) {
-    const int le = t / NFT;
-    const int r = t - le * NFT;
-    const int f = r / NFP;
-    const int fp = r - f * NFP;
+    int le, f, fp;
+    ftask.map(t, le, f, fp);
+    const int ti = le * NFT + f * NFP + fp;  // element-major index of the task
     int nM, nP, axis, sgi;
     face_nodes<NQ>(f, fp % NQ, fp / NQ, nM, nP, axis, sgi);
     const long long gM = g0 + (long long)le * NP + nM;
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS, emu_eo_min_blocks<P>())
     const double qM = qin[gM], qP = qin[gP];
     double tP, tM;
     if (fcin != nullptr) {
-      const double2 c = fcin[eb * NFT + t];
+      const double2 c = fcin[eb * NFT + ti];
       tP = c.x;
       tM = c.y;
     } else {
@@ -245,10 +245,10 @@ __global__ void __launch_bounds__(EmuEoCfg<P>::THREADS, emu_eo_min_blocks<P>())
       const double tw = (sgi > 0) ? 2.0 : -2.0;
       tP = fma(tw, uP, -a2);
       tM = fma(tw, uM, -a2);
-      if (fcout != nullptr) fcout[eb * NFT + t] = make_double2(tP, tM);
+      if (fcout != nullptr) fcout[eb * NFT + ti] = make_double2(tP, tM);
     }
     const dfl gf = df_scale2(df_split(fma(qP, tP, -(qM * tM))), 0.5f);
-    sg[t] = make_float2(gf.hi, gf.lo);
+    sg[ti] = make_float2(gf.hi, gf.lo);
   }
   // phase 1b: x pair values per (line, c < ceil(N/2)): the differences
   // G = q u - F0 by one FMA each, split, then S and Δ in double-float

@@ -328,26 +328,11 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   // before this one in the step stored them (FP64 body).
   const double2* __restrict__ fcin = reinterpret_cast<const double2*>(a.fc_in);
   double2* __restrict__ fcout = reinterpret_cast<double2*>(a.fc_out);
-  // Below p = 5 a face has fewer nodes than a warp has lanes: the tasks go
-  // face-major there (all elements' nodes of face 0, then face 1, ...), so
-  // that the face -- and the branch on it in face_nodes -- is the same for
-  // all lanes of a warp but at a face boundary.  f = t / (nloc*NFP) by a
-  // multiply-high with ceil(2^32 / W), exact for t*W < 2^32.
-  const unsigned fW = (unsigned)(nloc * NFP);
-  const unsigned fmagic = 0xFFFFFFFFu / fW + 1u;
+  // tasks face-major below p = 5 (FaceTasks)
+  const FaceTasks<NQ> ftask(nloc);
   for (int t = threadIdx.x; t < nloc * NFT; t += T) {
     int le, f, fp;
-    if constexpr (NFP < 32) {
-      f = (int)__umulhi((unsigned)t, fmagic);
-      const int rem = t - f * (int)fW;
-      le = rem / NFP;
-      fp = rem - le * NFP;
-    } else {
-      le = t / NFT;
-      const int rr = t - le * NFT;
-      f = rr / NFP;
-      fp = rr - f * NFP;
-    }
+    ftask.map(t, le, f, fp);
     const int r = f * NFP + fp;
     const int ti = le * NFT + r;  // the task's element-major index
     int nM, nP, axis, sg;
