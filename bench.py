@@ -408,6 +408,12 @@ def bench_ensemble(sdg, args):
         m0 = W.mass(q0[i], x, *m["dims"])
         drift.append(abs(W.mass(got, x, *m["dims"]) - m0) / abs(m0))
     launches = ens.launches_per_step()
+    # the same members with ONE persistent launch per RK stage over every order
+    ens.set_single_launch(True)
+    ens.step(args.warmup)
+    sdg.synchronize()
+    t1 = ens.step_timed(nst) / 1e3
+    launches1 = ens.launches_per_step()
     ens.close()
     per_solve = t / nst * args.ens_steps
     plain_per_solve = plain_t / plain_dof * dof  # all members, sequentially
@@ -424,6 +430,9 @@ def bench_ensemble(sdg, args):
         "ratio_vs_plain": plain_per_solve / per_solve,
         "rel_l2_vs_fp64_max": max(errs), "mass_drift_max": max(drift),
         "autotuned": cfg, "launches_per_step": launches,
+        "single_launch_per_stage": {"solves_per_s": args.ens_n / (t1 / nst * args.ens_steps),
+                                    "launches_per_step": launches1,
+                                    "ratio_to_per_order_launches": t / t1},
         "setup_s": time.perf_counter() - t0,
     }
 

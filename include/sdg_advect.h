@@ -486,6 +486,13 @@ int sdg_ensemble_get_threads(const sdg_ensemble* e, int* threads_by_order);
  * after the other on the ensemble's stream.  Results are the same either
  * way. */
 int sdg_ensemble_set_parallel_groups(sdg_ensemble* e, int on);
+/* on = 1: every RK stage is ONE persistent launch over the work items of all
+ * orders (blocks take items round-robin and switch on the item's order and
+ * body), three launches and the index advance a step; on = 0 (the default):
+ * one launch per order group and stage, each kernel compiled for its order
+ * with its own register budget, which measured faster.  Results are the same
+ * bit for bit either way. */
+int sdg_ensemble_set_single_launch(sdg_ensemble* e, int on);
 /* eo_by_order receives 12 entries (index = order): 1 where the order's
  * instances run the even-odd body, 0 for the node body or an absent order. */
 int sdg_ensemble_get_bodies(const sdg_ensemble* e, int* eo_by_order);

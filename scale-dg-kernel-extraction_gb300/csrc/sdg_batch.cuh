@@ -47,6 +47,8 @@ struct BatchItem {
   int inst;
   int e_begin;
   int e_count;
+  int body;  // 2 p + eo of the instance when the items were built: the stage
+             // body the single-launch kernel runs (the groups use the same)
 };
 
 // FP32 increment factors b_s*dt of the three SSP-RK3 stages (mod_common.f90:30).
@@ -109,6 +111,9 @@ struct BatchForkJoin {
   std::vector<cudaEvent_t> done;
   cudaEvent_t fork = nullptr;
   bool parallel = false;  // false: every group on the caller's stream
+  // true: each stage is ONE persistent launch over the items of every order
+  // (batch_stage_kernel), instead of one launch per order group
+  bool fused = false;
   BatchForkJoin() = default;
   BatchForkJoin(const BatchForkJoin&) = delete;
   BatchForkJoin& operator=(const BatchForkJoin&) = delete;

@@ -163,6 +163,47 @@ __global__ void __launch_bounds__(kBatchThreadsMax, batch_min_blocks<P, EO>())
   }
 }
 
+// ONE persistent launch per RK stage over the work items of every order:
+// blocks take items round-robin, read the item's instance header and run the
+// stage body compiled for that instance's order and body (a switch over the
+// 22 (order, body) pairs).  Block size and dynamic shared memory are the
+// largest the present orders need; each body takes the block size at run
+// time, so an item's bits are the per-order kernels'.  The kernel carries the
+// register needs of every body at once (capped at 64 for two blocks of 512
+// threads an SM), which is why the per-order launches are the default.
+template <int RK>
+__global__ void __launch_bounds__(kBatchThreadsMax, 2)
+    batch_stage_kernel(const BatchInst* __restrict__ insts, const BatchItem* __restrict__ items,
+                       int n_items, int stage) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ __align__(16) BatchInst s_inst;
+  __shared__ BatchItem s_item;
+  const int tid = threadIdx.x;
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    __syncthreads();  // the previous item's readers of s_inst / smem are done
+    if (tid == 0) s_item = items[it];
+    __syncthreads();
+    if (tid < kInstWords)
+      reinterpret_cast<uint32_t*>(&s_inst)[tid] =
+          reinterpret_cast<const uint32_t*>(insts + s_item.inst)[tid];
+    __syncthreads();
+    if (!s_inst.active) continue;  // uniform across the block
+    // the body recorded in the item, which the groups' shared-memory sizes
+    // were computed for (the device instance table's copy of the body flag
+    // is not refreshed when the body changes)
+    switch (s_item.body) {
+#define SDG_FUSED_CASE(P)                                                    \
+  case 2 * P: batch_item_body<P, 0, RK>(s_inst, s_item, stage, smem); break; \
+  case 2 * P + 1: batch_item_body<P, 1, RK>(s_inst, s_item, stage, smem); break;
+      SDG_FUSED_CASE(1) SDG_FUSED_CASE(2) SDG_FUSED_CASE(3) SDG_FUSED_CASE(4)
+      SDG_FUSED_CASE(5) SDG_FUSED_CASE(6) SDG_FUSED_CASE(7) SDG_FUSED_CASE(8)
+      SDG_FUSED_CASE(9) SDG_FUSED_CASE(10) SDG_FUSED_CASE(11)
+#undef SDG_FUSED_CASE
+      default: break;
+    }
+  }
+}
+
 __global__ void batch_advance_kernel(BatchInst* insts, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && insts[i].active) insts[i].cur = (insts[i].cur + 1) % 3;
@@ -336,9 +377,45 @@ BatchForkJoin::~BatchForkJoin() {
   if (fork) cudaEventDestroy(fork);
 }
 
+// The three stages as one persistent launch each over every group's items
+// (they are contiguous, sorted by order and body), then the index advance.
+static int batch_fused_enqueue(BatchInst* d_inst, int n_inst, const BatchItem* d_items,
+                               const std::vector<BatchGroup>& groups, cudaStream_t st) {
+  int n_items = 0, threads = 32;
+  size_t smem = 0;
+  for (const BatchGroup& g : groups) {
+    n_items = g.begin + g.count > n_items ? g.begin + g.count : n_items;
+    threads = g.threads > threads ? g.threads : threads;
+    smem = g.smem > smem ? g.smem : smem;
+  }
+  if (n_items > 0) {
+    SDG_TRY(set_kernel_smem((const void*)batch_stage_kernel<kRkFirst>, (int)smem, false));
+    SDG_TRY(set_kernel_smem((const void*)batch_stage_kernel<kRkGeneral>, (int)smem, false));
+    int dev = 0, nsm = 0, per_sm = 0;
+    SDG_CUDA_TRY(cudaGetDevice(&dev));
+    SDG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    SDG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, batch_stage_kernel<kRkGeneral>, threads, smem));
+    if (per_sm < 1)
+      return fail(SDG_ERR_INVALID_ARG, "the single-launch stage kernel does not fit an SM "
+                  "(%d threads, %zu bytes of shared memory)", threads, smem);
+    const long long cap = (long long)nsm * per_sm;
+    const int grid = (int)(n_items < cap ? n_items : cap);
+    for (int s = 0; s < 3; s++) {
+      if (s == 0)
+        batch_stage_kernel<kRkFirst><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, s);
+      else
+        batch_stage_kernel<kRkGeneral><<<grid, threads, smem, st>>>(d_inst, d_items, n_items, s);
+      SDG_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  return batch_advance_launch(d_inst, n_inst, st);
+}
+
 int batch_step_enqueue(BatchForkJoin& fj, BatchInst* d_inst, int n_inst,
                        const BatchItem* d_items, const std::vector<BatchGroup>& groups,
                        cudaStream_t st) {
+  if (fj.fused) return batch_fused_enqueue(d_inst, n_inst, d_items, groups, st);
   const size_t ng = groups.size();
   if (ng <= 1 || !fj.parallel) {
     for (int s = 0; s < 3; s++)

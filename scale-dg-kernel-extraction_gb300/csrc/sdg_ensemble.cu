@@ -63,7 +63,8 @@ int build_items(sdg_ensemble* e, const std::vector<int>* subset = nullptr) {
     const BatchInst& I = e->inst[i];
     const int epb = e->epb[I.p];
     for (long long b = 0; b < I.box.Ne; b += epb)
-      items.push_back({i, (int)b, (int)std::min<long long>(epb, I.box.Ne - b)});
+      items.push_back({i, (int)b, (int)std::min<long long>(epb, I.box.Ne - b),
+                       2 * I.p + (I.eo ? 1 : 0)});
   }
   cudaFree(e->d_items);
   e->d_items = nullptr;
@@ -329,6 +330,16 @@ int sdg_ensemble_set_parallel_groups(sdg_ensemble* e, int on) {
   return SDG_OK;
 }
 
+int sdg_ensemble_set_single_launch(sdg_ensemble* e, int on) {
+  if (!e) return fail(SDG_ERR_INVALID_ARG, "NULL ensemble");
+  e->fj.fused = (on != 0);
+  if (e->graph) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  return SDG_OK;
+}
+
 int sdg_ensemble_get_threads(const sdg_ensemble* e, int* threads_by_order) {
   if (!e || !threads_by_order) return fail(SDG_ERR_INVALID_ARG, "NULL argument");
   for (int p = 0; p <= kBatchMaxOrder; p++) threads_by_order[p] = e->threads[p];
@@ -456,7 +467,8 @@ int sdg_ensemble_download(sdg_ensemble* e, int i, double* q) {
 long long sdg_ensemble_total_dofs(const sdg_ensemble* e) { return e ? e->total_dof : 0; }
 
 int sdg_ensemble_launches_per_step(const sdg_ensemble* e) {
-  return e ? 3 * (int)e->groups.size() + 1 : 0;
+  if (!e) return 0;
+  return e->fj.fused ? 4 : 3 * (int)e->groups.size() + 1;
 }
 
 int sdg_ensemble_destroy(sdg_ensemble* e) {

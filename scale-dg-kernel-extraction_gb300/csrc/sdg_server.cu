@@ -145,7 +145,8 @@ int rebuild_tables(sdg_server* s) {
     const BatchInst& I = inst[i];
     const int e = s->epb[I.p];
     for (long long b = 0; b < I.box.Ne; b += e)
-      items.push_back({i, (int)b, (int)std::min<long long>(e, I.box.Ne - b)});
+      items.push_back({i, (int)b, (int)std::min<long long>(e, I.box.Ne - b),
+                       2 * I.p + (I.eo ? 1 : 0)});
   }
   // grow a table only once its new allocation has succeeded, so that a
   // failed allocation leaves the old table and its capacity consistent

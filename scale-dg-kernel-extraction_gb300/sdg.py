@@ -163,6 +163,7 @@ def _load() -> C.CDLL:
         "sdg_ensemble_set_order_threads": ([_vp, _i, _i], _i),
         "sdg_ensemble_get_threads": ([_vp, _ip], _i),
         "sdg_ensemble_set_parallel_groups": ([_vp, _i], _i),
+        "sdg_ensemble_set_single_launch": ([_vp, _i], _i),
         "sdg_ensemble_get_config": ([_vp, _ip, C.POINTER(_i), C.POINTER(_i)], _i),
         "sdg_ensemble_get_bodies": ([_vp, _ip], _i),
         "sdg_ensemble_step": ([_vp, _i], _i),
@@ -658,6 +659,12 @@ class Ensemble:
         """Order groups on parallel graph branches (True) or one stream."""
         _check(lib.sdg_ensemble_set_parallel_groups(self._h, int(bool(on))),
                "sdg_ensemble_set_parallel_groups")
+
+    def set_single_launch(self, on: bool) -> None:
+        """One persistent launch per RK stage over every order (True), or one
+        launch per order group and stage (False, the default)."""
+        _check(lib.sdg_ensemble_set_single_launch(self._h, int(bool(on))),
+               "sdg_ensemble_set_single_launch")
 
     def launches_per_step(self) -> int:
         return lib.sdg_ensemble_launches_per_step(self._h)

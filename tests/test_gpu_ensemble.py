@@ -186,3 +186,23 @@ def test_bad_ensemble_arguments_are_rejected():
     with pytest.raises(sdg.SdgError) as e:
         sdg.Ensemble([(2, 0, 2)], [3], [1e-3], ops)
     assert e.value.status == sdg.ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("opt", [sdg.OPT_EVENODD, sdg.OPT_GENERAL])
+def test_single_launch_per_stage_equals_the_per_order_launches(opt):
+    """One persistent launch per RK stage over every order (and body) gives
+    the per-order launches' bits; switching it on and off mid-run keeps the
+    state, and a step is then four launches."""
+    ens, fields, dts, ops = build(MEMBERS, seed0=300)
+    if opt != sdg.OPT_EVENODD:
+        ens.set_opt(opt)
+    ens.set_single_launch(True)
+    assert ens.launches_per_step() == 4
+    ens.step(2)
+    ens.set_single_launch(False)
+    ens.step(1)
+    ens.set_single_launch(True)
+    ens.step(1)
+    for i, (dims, p) in enumerate(MEMBERS):
+        want = standalone(dims, p, fields[i], dts[i], ops, 4, opt)
+        assert np.array_equal(ens.download(i), want), (i, dims, p)
