@@ -756,6 +756,9 @@ int sdg_slabs_create(sdg_slabs** out, int NeX, int NeY, int NeZ, int p, double L
     return fail(SDG_ERR_UNSUPPORTED_ORDER, "PolyOrder %d outside 1..15", p);
   if (NeX < 1 || NeY < 1 || NeZ < 1 || !(Lx > 0) || !(Ly > 0) || !(Lz > 0))
     return fail(SDG_ERR_INVALID_ARG, "bad box %dx%dx%d", NeX, NeY, NeZ);
+  if (nparts < 1 || nparts > NeZ)
+    return fail(SDG_ERR_INVALID_ARG, "cannot split %d element layers into %d slabs", NeZ,
+                nparts);
   if ((long long)NeX * NeY * (NeZ + 2LL * nparts) > 0x7fffffffLL)
     return fail(SDG_ERR_INVALID_ARG, "too many elements");
   if (opt != SDG_OPT_GENERAL && opt != SDG_OPT_OPT1 && opt != SDG_OPT_EVENODD)

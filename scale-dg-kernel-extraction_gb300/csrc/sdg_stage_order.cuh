@@ -7,6 +7,7 @@
 #include "sdg_stage_emu_eo.cuh"
 #include "sdg_stage_elem.cuh"
 #include "sdg_stage_eo.cuh"
+#include "sdg_stage_warp.cuh"
 
 namespace sdg {
 
@@ -24,6 +25,8 @@ int launch_stage_order(int prec, int opt, const StageArgs& a, cudaStream_t st) {
     // p = 1: one thread an element (same bits as the block body): 129.7
     // against 48.2 GDOF-updates/s at 128^3 on GB300
     if constexpr (P == 1) return launch_stage_elem_impl<P>(a, st);
+    // p = 2, 3: one warp an element (same bits as the block body)
+    if constexpr (P == 2 || P == 3) return launch_stage_warp_impl<P>(a, st);
     return launch_stage_eo_impl<P, float>(a, st);
   }
   if (prec == SDG_PREC_FP64) {

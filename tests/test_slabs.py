@@ -113,3 +113,12 @@ def test_exchange_fills_ghost_planes_across_two_ranks():
         assert p.exitcode == 0
     for rank, ok_lo, ok_hi, owned in res:
         assert ok_lo and ok_hi and owned, rank
+
+
+def test_create_rejects_bad_partition_counts_before_device_work():
+    from helpers import operators
+    _, D, _, L = operators(2)
+    for P in (0, -3, 5):
+        with pytest.raises(sdg.SdgError) as e:
+            sdg.Slabs(2, 2, 4, 2, D, L, P)
+        assert e.value.status == sdg.ERR_INVALID_ARG
