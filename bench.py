@@ -296,7 +296,9 @@ def roofline(precision, p, ne, ndof, t, steps, peaks, opt="opt1"):
     88.75 flops a DOF-update at p = 7).  `compute.frac` is that pipe's busy
     share from the kernel's ncu capture (sm__pipe_fp64_cycles_active);
     `achieved_tflops` counts the reference's formulas (25 + 6 Nq + 126 / Nq
-    flops a DOF-update) against the DFMA peak measured live."""
+    flops a DOF-update) against the DFMA peak measured live.  The FP32 and
+    emulated forms report those flops against the live FFMA peak, and the
+    emulated form its FP64 pipe's busy share apart (`fp64_pipe_busy`)."""
     launches = 3 * steps
     avg_launch = t / launches
     bpd = BYTES_PER_DOF_UPDATE[precision]
@@ -328,12 +330,18 @@ def roofline(precision, p, ne, ndof, t, steps, peaks, opt="opt1"):
                 "achieved_tflops": fl * per_gpu / 1e3,
                 "peak_tflops_measured_live": peaks[pipe]}
         busy = load_traffic(tkey, "fp64_pipe_active")
-        if busy is not None and precision in ("fp64", "fp64emu"):
+        if busy is not None and precision == "fp64":
             comp["frac"] = busy
             comp["frac_source"] = "sm__pipe_fp64_cycles_active, ncu capture of this kernel"
         else:
             comp["frac"] = fl * per_gpu / 1e3 / peaks[pipe]
             comp["frac_source"] = "reference-formula flops / live peak"
+            if busy is not None:
+                # the emulated form's FP64 work (face flux, RK combine) on
+                # the 1/64-rate pipe, beside its FP32 contraction
+                comp["fp64_pipe_busy"] = busy
+                comp["fp64_pipe_busy_source"] = ("sm__pipe_fp64_cycles_active, ncu capture "
+                                                 "of this kernel")
         roof["compute"] = comp
         if precision == "fp64":
             # the FP64 pipe binds when it is busier than HBM

@@ -132,3 +132,19 @@ def test_headline_line_is_compact(monkeypatch):
     assert line["gpu_launches"] == 150
     assert line["config"]["opt"] == "EVENODD"
     assert bench.config(args, reference=True)["opt"] == "OPT1"
+
+
+def test_emulated_roofline_reports_its_fp64_pipe_apart(monkeypatch):
+    """The emulated form's compute fraction is its FP32 flops against the
+    FFMA peak; the FP64 pipe's busy share from the capture sits beside it."""
+    monkeypatch.setattr(bench, "measured_peaks", lambda: (6000.0, "measured"))
+    p, ne, steps = 7, 32, 10
+    ndof = (p + 1) ** 3 * ne ** 3
+    t = 0.01
+    peaks = {"dfma_tflops": 1.25, "ffma_tflops": 75.0}
+    r = bench.roofline("fp64emu", p, ne, ndof, t, steps, peaks, "evenodd")
+    c = r["compute"]
+    assert c["pipe"] == "FP32 (FFMA)"
+    assert c["frac"] == pytest.approx(c["achieved_tflops"] / 75.0)
+    assert c["fp64_pipe_busy"] == pytest.approx(0.597)
+    assert "binding_roof" not in r

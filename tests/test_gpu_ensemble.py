@@ -206,3 +206,17 @@ def test_single_launch_per_stage_equals_the_per_order_launches(opt):
     for i, (dims, p) in enumerate(MEMBERS):
         want = standalone(dims, p, fields[i], dts[i], ops, 4, opt)
         assert np.array_equal(ens.download(i), want), (i, dims, p)
+
+
+def test_low_order_single_box_kernels_equal_the_block_body():
+    """The single-box FP32 even-odd stage runs its own kernels at p = 1..3
+    (an element a thread, the column form, a warp an element); the ensemble
+    runs the block body.  Element counts that fill no whole warp, boxes one
+    element wide and single elements included."""
+    members = [((2, 2, 2), 2), ((1, 3, 5), 2), ((4, 1, 1), 2), ((1, 1, 1), 3),
+               ((3, 5, 1), 3), ((2, 2, 2), 1), ((7, 1, 2), 2), ((1, 2, 7), 3)]
+    ens, fields, dts, ops = build(members, seed0=300)
+    ens.step(3)
+    for i, (dims, p) in enumerate(members):
+        want = standalone(dims, p, fields[i], dts[i], ops, 3)
+        assert np.array_equal(ens.download(i), want), (i, dims, p)

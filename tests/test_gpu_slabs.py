@@ -65,3 +65,12 @@ def test_bad_split_is_refused():
     with pytest.raises(sdg.SdgError) as e:
         sdg.Slabs(2, 2, 3, 2, c.D, c.Lift, 4)
     assert e.value.status == sdg.ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("p,dims,nparts", [(2, (3, 2, 5), 2), (2, (1, 3, 4), 3),
+                                           (3, (2, 1, 5), 2), (3, (5, 3, 3), 3)])
+def test_fp32_low_order_partitions(p, dims, nparts):
+    """The FP32 even-odd stage at p = 2 and 3 (the warp-cooperative kernels)
+    on partitions that start past element 0 of their extended box."""
+    _, a, b, _ = run_both(dims, p, nparts, sdg.OPT_EVENODD, sdg.PREC_FP32, 3)
+    assert np.array_equal(a, b)
