@@ -460,9 +460,11 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
 // Five measured faster on GB300 at most orders once stages 2-3 read the face
 // factors (1.02-1.06x up to p = 4, 1.005-1.013x at p = 6 and 8..13, 48
 // registers with small spills) and four at p = 5, 7, 14 and 15 (by 0.2-1.1 %).
+// At p = 1 eight blocks (32 registers, 68 bytes of spills) measured 20.5
+// against 19.8 GDOF-updates/s for five (20.4 for six); at p = 2 six were level.
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_min_blocks() {
-  if (sizeof(CT) == 8) return (P == 5 || P == 7 || P >= 14) ? 4 : 5;
+  if (sizeof(CT) == 8) return (P == 5 || P == 7 || P >= 14) ? 4 : P == 1 ? 8 : 5;
   if (P == 4) return 6;  // 40 registers, one thread a line (above)
   return (P <= 3 || P == 5 || eo_lines<P, CT>() == 128) ? 8 : P <= 12 ? 4 : 3;
 }
