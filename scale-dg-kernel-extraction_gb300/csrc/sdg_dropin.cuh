@@ -39,10 +39,14 @@ struct TendArgs {
   long long NpNeA;      // Np*NeA: valid 1-based indices are 1..NpNeA
 };
 
+// Elements per block: as many whole elements as the block has threads for
+// (32 at p = 1, 9 at p = 2, 4 at p = 3, 2 at p = 4, one from p = 5), so that
+// every thread owns a node at low orders; R nodes a thread in all.
 template <int P>
 struct DropCfg {
-  static constexpr int EPB = (P <= 2) ? 8 : (P <= 4) ? 2 : 1;
   static constexpr int THREADS = (P >= 10) ? 512 : 256;
+  static constexpr int EPB = (THREADS / Ord<P>::NP) > 0 ? THREADS / Ord<P>::NP : 1;
+  static constexpr int R = (EPB * Ord<P>::NP + THREADS - 1) / THREADS;
 };
 
 template <int P>
@@ -81,17 +85,43 @@ __global__ void __launch_bounds__(DropCfg<P>::THREADS) dqdt_kernel(const TendArg
   }
   __syncthreads();
   const long long NpNe = (long long)NP * a.Ne;
-  for (int t = threadIdx.x; t < nloc * NP; t += T) {
-    const int le = t / NP;
-    const int n = t - le * NP;
-    const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
-    const double dx = line_sum<NQ, SPLIT3, NQ>(sD + i, fx + le * NP + j * NQ + k * NQ2, 1);
-    const double dy = line_sum<NQ, SPLIT3, 1>(sDt + j * NQ, fy + le * NP + i + k * NQ2, NQ);
-    const double dz = line_sum<NQ, SPLIT3, 1>(sDt + k * NQ, fz + le * NP + i + j * NQ, NQ2);
-    const double lf = lift_node<P>(a.Lift + n, a.flux + (eb + le) * NFT, i, j, k);
-    const long long g = g0 + t;
-    a.dqdt[g] = -(((a.Escale[g] * dx + a.Escale[g + NpNe] * dy) +
-                   a.Escale[g + 2 * NpNe] * dz) + lf);
+  // one direction at a time, each node's running sum
+  // Escale_x D F_x + Escale_y D F_y + Escale_z D F_z kept in acc: a thread
+  // keeps one line sum live, not three (94 registers and two blocks an SM at
+  // p = 3 with the three interleaved)
+  constexpr int R = DropCfg<P>::R;
+  double acc[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int t = threadIdx.x + r * T;
+    if (t < nloc * NP) {
+      const int le = t / NP, n = t - le * NP;
+      const int j = (n / NQ) % NQ, k = n / NQ2;
+      const double dx =
+          line_sum<NQ, SPLIT3, NQ>(sD + n % NQ, fx + le * NP + j * NQ + k * NQ2, 1);
+      acc[r] = a.Escale[g0 + t] * dx;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int t = threadIdx.x + r * T;
+    if (t < nloc * NP) {
+      const int le = t / NP, n = t - le * NP;
+      const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
+      const double dy = line_sum<NQ, SPLIT3, 1>(sDt + j * NQ, fy + le * NP + i + k * NQ2, NQ);
+      acc[r] = fma(a.Escale[g0 + t + NpNe], dy, acc[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int t = threadIdx.x + r * T;
+    if (t < nloc * NP) {
+      const int le = t / NP, n = t - le * NP;
+      const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
+      const double dz = line_sum<NQ, SPLIT3, 1>(sDt + k * NQ, fz + le * NP + i + j * NQ, NQ2);
+      const double lf = lift_node<P>(a.Lift + n, a.flux + (eb + le) * NFT, i, j, k);
+      a.dqdt[g0 + t] = -(fma(a.Escale[g0 + t + 2 * NpNe], dz, acc[r]) + lf);
+    }
   }
 }
 
@@ -345,13 +375,22 @@ __global__ void __launch_bounds__(DropCfg<P>::THREADS) divlike_kernel(const DivA
     fz[t] = a.iz[g0 + t];
   }
   __syncthreads();
+  // one direction at a time (a thread keeps one line sum live; 74 registers
+  // at p = 3 with the three interleaved)
   for (int t = threadIdx.x; t < nloc * NP; t += T) {
-    const int le = t / NP;
-    const int n = t - le * NP;
+    const int le = t / NP, n = t - le * NP;
+    const int j = (n / NQ) % NQ, k = n / NQ2;
+    a.ox[g0 + t] = line_sum<NQ, SPLIT3, NQ>(sD + n % NQ, fx + le * NP + j * NQ + k * NQ2, 1);
+  }
+  for (int t = threadIdx.x; t < nloc * NP; t += T) {
+    const int le = t / NP, n = t - le * NP;
     const int i = n % NQ, j = (n / NQ) % NQ, k = n / NQ2;
-    a.ox[g0 + t] = line_sum<NQ, SPLIT3, NQ>(sD + i, fx + le * NP + j * NQ + k * NQ2, 1);
     a.oy[g0 + t] = line_sum<NQ, SPLIT3, 1>(sDt + j * NQ, fy + le * NP + i + k * NQ2, NQ);
-    a.oz[g0 + t] = line_sum<NQ, SPLIT3, 1>(sDt + k * NQ, fz + le * NP + i + j * NQ, NQ2);
+  }
+  for (int t = threadIdx.x; t < nloc * NP; t += T) {
+    const int le = t / NP, n = t - le * NP;
+    const int i = n % NQ, j = (n / NQ) % NQ;
+    a.oz[g0 + t] = line_sum<NQ, SPLIT3, 1>(sDt + (n / NQ2) * NQ, fz + le * NP + i + j * NQ, NQ2);
   }
 }
 
