@@ -230,7 +230,9 @@ __device__ __forceinline__ void eo_pairs_f64(const double* __restrict__ q,
 // the RK combination in FP64.  Block size and nloc are runtime values, so the
 // batched persistent kernel can use the same body.
 // PREF (FP32 body): start q0 towards L2 in phase 0 and unroll the staging
-// loop by 4, so more loads are in flight per warp.  Measured on GB300 for the
+// loop by 4, so more loads are in flight per warp.  (Four nodes a thread as
+// 16-byte loads measured 0.93-0.98x at p = 5..11: the stores of four
+// consecutive nodes a thread hit the same shared-memory banks.)  Measured on GB300 for the
 // single-box kernel: 1.03-1.06x at p >= 4 (103 GDOF-updates/s at p = 7),
 // 0.95x at p = 1; in the batched kernel it was 0.8-0.9x, so it stays off there.
 template <int P, typename CT, int RKFIX = -1, bool FLY = false, bool PREF = false,
