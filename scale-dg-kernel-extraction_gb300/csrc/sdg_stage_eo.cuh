@@ -89,6 +89,11 @@ __host__ __device__ constexpr int eo_lines() {
 // The FP32 body at p = 5 runs 4 elements (144 lines, two threads a line) on
 // 256 threads, eight blocks an SM: 1.07x the 512-thread shape (79.1 against
 // 73.6 GDOF-updates/s); the same at p = 4 and 6 was level or slower.
+template <int P, typename CT>
+__host__ __device__ constexpr bool eo_exact() {
+  return sizeof(CT) == 4 && (P == 11 || P == 12);
+}
+
 template <int P, typename CT = double>
 struct EoCfg {
   static constexpr bool SMALL5 = sizeof(CT) == 4 && P == 5;
@@ -96,8 +101,9 @@ struct EoCfg {
   // lines (288 and 352 threads) instead of 512 threads of which 288 / 338
   // had a line; measured on GB300 90.2 against 86.7 and 80.3 against 74.6
   // GDOF-updates/s (at p = 13 and 14 the 512-thread shape stays faster:
-  // 78.2 against 77.3, 72.1 against 71.6)
-  static constexpr bool EXACT = sizeof(CT) == 4 && (P == 11 || P == 12);
+  // 78.2 against 77.3, 72.1 against 71.6; at p = 9 level, 87.0 against 86.5;
+  // the FP64 form at p = 11..13, bound by its FP64 pipe, level too)
+  static constexpr bool EXACT = eo_exact<P, CT>();
   static constexpr int LINES = eo_lines<P, CT>();
   static constexpr int THREADS =
       SMALL5 ? 256
