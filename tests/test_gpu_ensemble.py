@@ -220,3 +220,15 @@ def test_low_order_single_box_kernels_equal_the_block_body():
     for i, (dims, p) in enumerate(members):
         want = standalone(dims, p, fields[i], dts[i], ops, 3)
         assert np.array_equal(ens.download(i), want), (i, dims, p)
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_low_order_kernels_on_a_box_past_the_32_bit_index_constants(p):
+    """4096 x 16 x 16 elements: e * NeX reaches 2^32, so the single-box p = 2
+    and 3 kernels find element coordinates by division instead of the 32-bit
+    multiply-high constants; the result still equals the block body's."""
+    members = [((4096, 16, 16), p)]
+    ens, fields, dts, ops = build(members, seed0=400)
+    ens.step(1)
+    want = standalone(members[0][0], p, fields[0], dts[0], ops, 1)
+    assert np.array_equal(ens.download(0), want)
