@@ -80,10 +80,14 @@ __host__ __device__ constexpr int eo_parts() {
 
 // Lines of a block: 256, or 128 for the FP32 body at p = 7, 9 and 10, where
 // twice as many half-size blocks (the same 64 warps an SM) measured 1.04-1.05x
-// on GB300 (108 against 103 GDOF-updates/s at p = 7; 0.95x at p = 8).
+// on GB300 (108 against 103 GDOF-updates/s at p = 7; 0.95x at p = 8), and for
+// the FP64 body at p = 7 (eight blocks of 128 threads for four of 256, the
+// same 61 registers: 19.81 against 19.68 GDOF-updates/s).
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_lines() {
-  return (sizeof(CT) == 4 && (P == 7 || P == 9 || P == 10)) ? 128 : 256;
+  return ((sizeof(CT) == 4 && (P == 7 || P == 9 || P == 10)) || (sizeof(CT) == 8 && P == 7))
+             ? 128
+             : 256;
 }
 
 // The FP32 body at p = 5 runs 4 elements (144 lines, two threads a line) on
@@ -480,9 +484,11 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
 // registers with small spills) and four at p = 5, 7, 14 and 15 (by 0.2-1.1 %).
 // At p = 1 eight blocks (32 registers, 68 bytes of spills) measured 20.5
 // against 19.8 GDOF-updates/s for five (20.4 for six); at p = 2 six were level.
+// At p = 7 the blocks have 128 threads (eo_lines), so four blocks' worth of
+// warps is eight blocks (ten, at 48 registers with spills: 19.75).
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_min_blocks() {
-  if (sizeof(CT) == 8) return (P == 5 || P == 7 || P >= 14) ? 4 : P == 1 ? 8 : 5;
+  if (sizeof(CT) == 8) return P == 7 ? 8 : (P == 5 || P >= 14) ? 4 : P == 1 ? 8 : 5;
   if (P == 4) return 6;  // 40 registers, one thread a line (above)
   if (P == 11) return 3;  // 288 threads, 56 registers (exact-size blocks, EoCfg)
   if (P == 12) return 4;  // 352 threads, 40 registers
