@@ -82,7 +82,8 @@ __host__ __device__ constexpr int eo_parts() {
 // twice as many half-size blocks (the same 64 warps an SM) measured 1.04-1.05x
 // on GB300 (108 against 103 GDOF-updates/s at p = 7; 0.95x at p = 8), and for
 // the FP64 body at p = 7 (eight blocks of 128 threads for four of 256, the
-// same 61 registers: 19.81 against 19.68 GDOF-updates/s).
+// same 61 registers: 19.81 against 19.68 GDOF-updates/s; at p = 1..5 the
+// same change measured 0.97-1.008x).
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_lines() {
   return ((sizeof(CT) == 4 && (P == 7 || P == 9 || P == 10)) || (sizeof(CT) == 8 && P == 7))
