@@ -72,10 +72,13 @@ struct EoShape {
 // and keeps one.  The batched kernels pick their own count (batch_eo_parts).
 // At p = 4 and 6 one thread a line measured faster (77.5 against 70.0
 // GDOF-updates/s at p = 4 with 256 threads and six blocks an SM; 77.3 against
-// 69.1 at p = 6 with four), at p = 5 slower (78.2 against 80.0).
+// 69.1 at p = 6 with four), at p = 5 slower (78.2 against 80.0); likewise at
+// p = 11..14 with the block counts of eo_min_blocks (92.3 against 90.0, 88.4
+// against 80.1, 87.9 against 78.2, 82.7 against 72.1), level or slower at
+// p = 8..10 and 15.
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_parts() {
-  return (sizeof(CT) == 4 && P >= 4 && P != 4 && P != 6) ? 2 : 1;
+  return (sizeof(CT) == 4 && P >= 5 && P != 6 && (P < 11 || P > 14)) ? 2 : 1;
 }
 
 // Lines of a block: 256, or 128 for the FP32 body at p = 7, 9 and 10, where
@@ -103,11 +106,12 @@ template <int P, typename CT = double>
 struct EoCfg {
   static constexpr bool SMALL5 = sizeof(CT) == 4 && P == 5;
   // FP32 at p = 11 and 12: one element a block, the block sized to its
-  // lines (288 and 352 threads) instead of 512 threads of which 288 / 338
-  // had a line; measured on GB300 90.2 against 86.7 and 80.3 against 74.6
-  // GDOF-updates/s (at p = 13 and 14 the 512-thread shape stays faster:
-  // 78.2 against 77.3, 72.1 against 71.6; at p = 9 level, 87.0 against 86.5;
-  // the FP64 form at p = 11..13, bound by its FP64 pipe, level too)
+  // lines instead of 256 lines of which 144 / 169 had work; measured on
+  // GB300 with two threads a line 90.2 against 86.7 and 80.3 against 74.6
+  // GDOF-updates/s (now one thread a line, eo_parts: 160 and 192 threads).
+  // At p = 13 and 14 the 256-line shape stays faster (78.2 against 77.3,
+  // 72.1 against 71.6 with two threads a line), at p = 9 level (87.0 against
+  // 86.5), and the FP64 form at p = 11..13, bound by its FP64 pipe, level.
   static constexpr bool EXACT = eo_exact<P, CT>();
   static constexpr int LINES = eo_lines<P, CT>();
   static constexpr int THREADS =
@@ -491,8 +495,11 @@ template <int P, typename CT>
 __host__ __device__ constexpr int eo_min_blocks() {
   if (sizeof(CT) == 8) return P == 7 ? 8 : (P == 5 || P >= 14) ? 4 : P == 1 ? 8 : 5;
   if (P == 4) return 6;  // 40 registers, one thread a line (above)
-  if (P == 11) return 3;  // 288 threads, 56 registers (exact-size blocks, EoCfg)
-  if (P == 12) return 4;  // 352 threads, 40 registers
+  // one thread a line from p = 11 to 14 (eo_parts); p = 11, 12 in blocks
+  // sized to one element's lines (EoCfg: 160 and 192 threads)
+  if (P == 11) return 5;
+  if (P == 12 || P == 13) return 6;
+  if (P == 14) return 4;
   return (P <= 3 || P == 5 || eo_lines<P, CT>() == 128) ? 8 : P <= 12 ? 4 : 3;
 }
 
