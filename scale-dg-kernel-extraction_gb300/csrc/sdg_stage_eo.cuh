@@ -72,13 +72,14 @@ struct EoShape {
 // and keeps one.  The batched kernels pick their own count (batch_eo_parts).
 // At p = 4 and 6 one thread a line measured faster (77.5 against 70.0
 // GDOF-updates/s at p = 4 with 256 threads and six blocks an SM; 77.3 against
-// 69.1 at p = 6 with four), at p = 5 slower (78.2 against 80.0); likewise at
-// p = 11..14 with the block counts of eo_min_blocks (92.3 against 90.0, 88.4
-// against 80.1, 87.9 against 78.2, 82.7 against 72.1), level or slower at
-// p = 8..10 and 15.
+// 69.1 at p = 6 with four); likewise at p = 5 with five blocks of 256 threads
+// (81.5 against 79.6 for four elements on 256 threads with two threads a
+// line) and at p = 11..14 with the block counts of eo_min_blocks (92.3
+// against 90.0, 88.4 against 80.1, 87.9 against 78.2, 82.7 against 72.1);
+// level or slower at p = 8..10 and 15.
 template <int P, typename CT>
 __host__ __device__ constexpr int eo_parts() {
-  return (sizeof(CT) == 4 && P >= 5 && P != 6 && (P < 11 || P > 14)) ? 2 : 1;
+  return (sizeof(CT) == 4 && P >= 7 && (P < 11 || P > 14)) ? 2 : 1;
 }
 
 // Lines of a block: 256, or 128 for the FP32 body at p = 7, 9 and 10, where
@@ -94,9 +95,6 @@ __host__ __device__ constexpr int eo_lines() {
              : 256;
 }
 
-// The FP32 body at p = 5 runs 4 elements (144 lines, two threads a line) on
-// 256 threads, eight blocks an SM: 1.07x the 512-thread shape (79.1 against
-// 73.6 GDOF-updates/s); the same at p = 4 and 6 was level or slower.
 template <int P, typename CT>
 __host__ __device__ constexpr bool eo_exact() {
   return sizeof(CT) == 4 && (P == 11 || P == 12);
@@ -104,7 +102,6 @@ __host__ __device__ constexpr bool eo_exact() {
 
 template <int P, typename CT = double>
 struct EoCfg {
-  static constexpr bool SMALL5 = sizeof(CT) == 4 && P == 5;
   // FP32 at p = 11 and 12: one element a block, the block sized to its
   // lines instead of 256 lines of which 144 / 169 had work; measured on
   // GB300 with two threads a line 90.2 against 86.7 and 80.3 against 74.6
@@ -114,12 +111,9 @@ struct EoCfg {
   // 86.5), and the FP64 form at p = 11..13, bound by its FP64 pipe, level.
   static constexpr bool EXACT = eo_exact<P, CT>();
   static constexpr int LINES = eo_lines<P, CT>();
-  static constexpr int THREADS =
-      SMALL5 ? 256
-      : EXACT ? ((Ord<P>::NQ2 * eo_parts<P, CT>() + 31) / 32) * 32
-              : LINES * eo_parts<P, CT>();
-  static constexpr int EPB = (SMALL5 ? 4 : EXACT ? 1
-                              : (LINES / Ord<P>::NQ2) > 0 ? LINES / Ord<P>::NQ2 : 1);
+  static constexpr int THREADS = EXACT ? ((Ord<P>::NQ2 * eo_parts<P, CT>() + 31) / 32) * 32
+                                       : LINES * eo_parts<P, CT>();
+  static constexpr int EPB = EXACT ? 1 : (LINES / Ord<P>::NQ2) > 0 ? LINES / Ord<P>::NQ2 : 1;
 };
 
 // Dynamic shared memory of one block with nloc elements: the three scaled
@@ -476,12 +470,13 @@ __device__ __forceinline__ void stage_eo_block(const StageArgs& a, long long eb,
   });
 }
 
-// Resident blocks an SM.  FP32 (512 threads; 256 up to p = 3 and at p = 7,
-// 9, 10, with twice the blocks): the body
-// issues few instructions per byte and needs warps to hide memory latency, so
-// up to p = 12 the registers are capped at 32 for 64 warps (measured 1.0-1.16x
-// the three-block build, 100 against 91.5 GDOF-updates/s at p = 7); above
-// that shared memory admits three blocks and the cap would only spill.
+// Resident blocks an SM.  FP32, two threads a line (512 threads, or 256 at
+// p = 7, 9, 10 with twice the blocks): the body issues few instructions per
+// byte and needs warps to hide memory latency, so the registers are capped at
+// 32 for 64 warps (measured 1.0-1.16x the three-block build, 100 against 91.5
+// GDOF-updates/s at p = 7); at p = 15 shared memory admits three blocks and
+// the cap would only spill.  One thread a line (p <= 6 and 11..14): the
+// counts below, each measured on GB300 against its neighbours.
 // FP64: four or five blocks of 256 threads (registers capped at 64 or 48): a
 // block in its load or flux phase leaves the others feeding the FP64 pipe.
 // Five measured faster on GB300 at most orders once stages 2-3 read the face
@@ -495,12 +490,13 @@ template <int P, typename CT>
 __host__ __device__ constexpr int eo_min_blocks() {
   if (sizeof(CT) == 8) return P == 7 ? 8 : (P == 5 || P >= 14) ? 4 : P == 1 ? 8 : 5;
   if (P == 4) return 6;  // 40 registers, one thread a line (above)
+  if (P == 5) return 5;  // 48 registers, one thread a line
   // one thread a line from p = 11 to 14 (eo_parts); p = 11, 12 in blocks
   // sized to one element's lines (EoCfg: 160 and 192 threads)
   if (P == 11) return 5;
   if (P == 12 || P == 13) return 6;
   if (P == 14) return 4;
-  return (P <= 3 || P == 5 || eo_lines<P, CT>() == 128) ? 8 : P <= 12 ? 4 : 3;
+  return (P <= 3 || eo_lines<P, CT>() == 128) ? 8 : P <= 12 ? 4 : 3;
 }
 
 // FP32 single-box kernel: F_y / F_z formed on the fly (FLY) at the orders
