@@ -186,9 +186,21 @@ def test_fp32_evenodd_tendency(p):
     assert rel_l2(dq, c.oracle_tend()) <= TOL_FP32
 
 
+@pytest.mark.parametrize("p", [1, 2, 3, 5, 7, 11, 12, 13, 14])
+def test_fp32_evenodd_steps(p):
+    """The RK stages of the FP32 even-odd kernels (each order's own shape:
+    an element a thread, the warp forms, one or two threads a line, blocks
+    sized to an element) against the FP64 oracle's steps."""
+    c = Case(*mesh_dims(p), p, ic="blob")
+    s = solver_for(c, opt=sdg.OPT_EVENODD, prec=sdg.PREC_FP32)
+    s.step(c.dt, 3)
+    assert rel_l2(s.download(), c.oracle_run(3)) <= TOL_FP32
+
+
 @pytest.mark.parametrize("prec,opt", [(sdg.PREC_FP64, sdg.OPT_OPT1),
                                       (sdg.PREC_FP64, sdg.OPT_EVENODD),
                                       (sdg.PREC_FP32, sdg.OPT_OPT1),
+                                      (sdg.PREC_FP32, sdg.OPT_EVENODD),
                                       (sdg.PREC_FP64_EMU, sdg.OPT_OPT1),
                                       (sdg.PREC_FP64_EMU, sdg.OPT_EVENODD)])
 @pytest.mark.parametrize("nstep", [1, 2, 3])
