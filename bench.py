@@ -316,7 +316,10 @@ def roofline(precision, p, ne, ndof, t, steps, peaks, opt="opt1"):
     elif precision == "fp64emu" and opt == "evenodd":
         kernel, tkey = f"stage_emu_eo_kernel<{p}>", f"stage_fp64emueo_p{p}_ne{ne}"
     elif precision == "fp32" and opt == "evenodd":
-        kernel, tkey = f"stage_eo_kernel<{p},float>", f"stage_fp32eo_p{p}_ne{ne}"
+        # the single box's own kernels at the lowest orders (same arithmetic)
+        k32 = {1: "stage_p1_kernel", 2: "stage_col_kernel<2>", 3: "stage_p3_kernel"}
+        kernel = k32.get(p, f"stage_eo_kernel<{p},float>")
+        tkey = f"stage_fp32eo_p{p}_ne{ne}"
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak,
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
