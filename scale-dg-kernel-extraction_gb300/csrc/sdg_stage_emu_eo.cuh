@@ -35,11 +35,12 @@ namespace sdg {
 
 // Lines a block aims at: 256, or 128 at p = 7, where twice as many half-size
 // blocks (the same warps an SM) measured 1.05x on GB300 (0.89-0.99x at p = 5,
-// 9 and 10).
+// 9 and 10), and at p <= 4 with twelve blocks an SM (1.04-1.06x: 32.0
+// against 30.2 GDOF-updates/s at p = 1, 44.6 against 42.4 at p = 3).
 template <int P>
 struct EmuEoCfg {
   static constexpr int NQ2 = (P + 1) * (P + 1);
-  static constexpr int AIM = (P == 7) ? 128 : 256;
+  static constexpr int AIM = (P == 7 || P <= 4) ? 128 : 256;
   static constexpr int EPB = (AIM / NQ2) > 0 ? (AIM / NQ2) : 1;
   static constexpr int LINES = EPB * NQ2;
   static constexpr int THREADS = ((LINES + 31) / 32) * 32;
@@ -156,14 +157,14 @@ __device__ __forceinline__ void emu_eo_line(const float2* row, const float2* __r
 }
 
 // Resident blocks of about 256 threads an SM the registers are capped for
-// (twice as many at p = 7, of 128).  The body waits on both the FP64 pipe
+// (twice as many of 128 at p <= 4 and p = 7).  The body waits on both the FP64 pipe
 // and instruction issue, and more warps overlap the two: measured on GB300,
 // six blocks (40 registers) up to p = 6 and five (48 registers, no spills) up
 // to p = 12 run 1.07-1.14x four blocks; above p = 12 the caps spill and four
 // blocks are faster.
 template <int P>
 __host__ __device__ constexpr int emu_eo_min_blocks() {
-  return P <= 6 ? 6 : P == 7 ? 10 : (P <= 12 ? 5 : 4);
+  return P <= 4 ? 12 : P <= 6 ? 6 : P == 7 ? 10 : (P <= 12 ? 5 : 4);
 }
 
 template <int P>
