@@ -501,7 +501,8 @@ __host__ __device__ constexpr int eo_min_blocks() {
 
 // FP32 single-box kernel: F_y / F_z formed on the fly (FLY) at the orders
 // where that measured faster on GB300 (1.07-1.18x at p = 10, 13 and 15, even
-// at 12 and 14); staging them is faster below (up to 1.15x at p = 6).
+// at 12 and 14); staging them is faster below (up to 1.15x at p = 6;
+// rechecked with the current shapes at p = 4, 6 and 8: FLY 0.92-0.99x).
 template <int P>
 __host__ __device__ constexpr bool eo_fly_single() {
   return P == 10 || P >= 12;
