@@ -27,8 +27,9 @@ def test_multiply_high_matches_division_in_its_range():
 def test_the_kernels_fall_back_outside_it():
     """d = 1 has no 32-bit constant (the kernels divide then), and past
     e * d = 2^32 the quotient can be one too large: with d = 3 (r = m d - 2^32
-    = 2) it is at e = 2^31 + 2, the first e >= 2^31 with e mod 3 = 2."""
+    = 2) it is at e = 2^31, where e / d + e r / (d 2^32) reaches the next
+    integer."""
     assert (0xFFFFFFFF // 1 + 1) & 0xFFFFFFFF == 0
-    e, d = (1 << 31) + 2, 3
+    e, d = 1 << 31, 3
     assert e % d == d - 1 and e * d >= 1 << 32
     assert umulhi_div(e, d) == e // d + 1
