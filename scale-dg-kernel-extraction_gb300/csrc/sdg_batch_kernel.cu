@@ -45,7 +45,9 @@ __host__ __device__ constexpr bool batch_eo_fly() {
 
 // Even-odd body: threads a line.  One up to p = 4, where a line has at most
 // two output pairs (measured in the batch on GB300: p = 3 81.5 against 75.3,
-// p = 4 82.1 against 71.6 GDOF-updates/s), two above.
+// p = 4 82.1 against 71.6 GDOF-updates/s), two above (one at p = 5 with 64
+// registers measured 439 against 450 solves/s on the 256-member ensemble,
+// and at p = 11 level on the serving stream).
 template <int P>
 __host__ __device__ constexpr int batch_eo_parts() {
   return P <= 4 ? 1 : 2;
